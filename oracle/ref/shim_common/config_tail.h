@@ -1,0 +1,26 @@
+/* Macros the reference sources reference but the golden-vector configs do not
+ * vary (unicycle / Dubins constants, reduction sizes, verbosity). */
+#pragma once
+#define W_R1_SIZE ((W_MAX - W_MIN) / W_R1_LENGTH)
+#define C_R1_SIZE ((C_MAX - C_MIN) / C_R1_LENGTH)
+#define V_R1_SIZE ((V_MAX - V_MIN) / V_R1_LENGTH)
+#define W_R1_VOL (W_R1_SIZE * W_R1_SIZE * W_R1_SIZE)
+#define NUM_R1_REGIONS (W_R1_LENGTH * W_R1_LENGTH * W_R1_LENGTH)
+#define NUM_R2_PER_R1 (W_R2_LENGTH * W_R2_LENGTH * W_R2_LENGTH)
+#define NUM_R2_REGIONS (NUM_R1_REGIONS * NUM_R2_PER_R1)
+#define NUM_R1_REGIONS_KERNEL1 1024
+#define NUM_PARTIAL_SUMS 1024
+#define EPSILON 1e-2f
+#define VERBOSE 0
+#define UNI_MIN_STEERING -M_PI / 2
+#define UNI_MAX_STEERING M_PI / 2
+#define UNI_MIN_DT 0.1f
+#define UNI_MAX_DT 2.0f
+#define UNI_LENGTH 1.0f
+#define DUBINS_AIRPLANE_MIN_PR (-M_PI / 4)
+#define DUBINS_AIRPLANE_MAX_PR (M_PI / 4)
+#define DUBINS_AIRPLANE_MIN_YR (-M_PI / 4)
+#define DUBINS_AIRPLANE_MAX_YR (M_PI / 4)
+#define DUBINS_AIRPLANE_MIN_PITCH -M_PI / 3
+#define DUBINS_AIRPLANE_MAX_PITCH M_PI / 3
+#define KM 0.03f
