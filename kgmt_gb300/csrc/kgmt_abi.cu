@@ -1,0 +1,607 @@
+// kgmt_abi.cu -- the C ABI (include/kgmt.h): single planner, batch, server
+// and the function-level propagation entry.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <new>
+#include <vector>
+
+#include "../../include/kgmt.h"
+#include "kgmt_engine.h"
+
+using namespace kgmt;
+
+namespace kgmt {
+extern thread_local std::string g_last_error;
+}
+
+#define RETURN_IF(cond, code, msg) \
+    do {                           \
+        if(cond)                   \
+            {                      \
+                set_error(msg);    \
+                return code;       \
+            }                      \
+    } while(0)
+
+#define CHECK_ST(expr)                      \
+    do {                                    \
+        kgmt_status st_ = (expr);           \
+        if(st_ != KGMT_OK) return st_;      \
+    } while(0)
+
+// ---------------------------------------------------------------------------
+// library
+// ---------------------------------------------------------------------------
+extern "C" const char* kgmt_version(void) { return "kgmt-gb300 1.0 (sm_103a)"; }
+
+extern "C" const char* kgmt_last_error(void) { return kgmt::g_last_error.c_str(); }
+
+extern "C" int32_t kgmt_sample_dim(int32_t model)
+{
+    if(model != KGMT_MODEL_DOUBLE_INTEGRATOR && model != KGMT_MODEL_QUADROTOR) return -1;
+    return (int32_t)sample_dim_of(model);
+}
+
+extern "C" kgmt_status kgmt_config_default(int32_t model, kgmt_config* out)
+{
+    RETURN_IF(!out, KGMT_ERR_INVALID_ARG, "kgmt_config_default: out is NULL");
+    kgmt_config c;
+    std::memset(&c, 0, sizeof(c));
+    c.model = model;
+    c.di_rule = KGMT_DI_RULE_RK4;
+    c.epsilon = 1e-2f;
+    c.ws_min = 0.0f;
+    c.ws_max = 1.0f;
+    c.goal_radius = 0.05f;
+    c.v_min = -0.3f;
+    c.v_max = 0.3f;
+    c.nu = 10e-3f;
+    c.mu = 2e-6f;
+    c.ix = 1.0f;
+    c.iy = 1.0f;
+    c.iz = 2.0f;
+    c.mass_inv = 1.0f;
+    c.seed = 1;
+    if(model == KGMT_MODEL_DOUBLE_INTEGRATOR)
+        {
+            c.tree_capacity = 100000;
+            c.samples_per_node = 4;
+            c.max_iterations = 200;
+            c.min_steps = 1;
+            c.max_steps = 6;
+            c.step_size = 0.05f;
+            c.coarse_len = 8;
+            c.fine_len = 2;
+            for(int i = 0; i < 3; ++i) c.u_min[i] = -1.0f, c.u_max[i] = 1.0f;
+            c.gravity = -9.81f;
+        }
+    else if(model == KGMT_MODEL_QUADROTOR)
+        {
+            const float pi = 3.14159265358979323846f;
+            c.tree_capacity = 2000000;
+            c.samples_per_node = 8;
+            c.max_iterations = 200;
+            c.min_steps = 3;
+            c.max_steps = 15;
+            c.step_size = 0.02f;
+            c.coarse_len = 16;
+            c.fine_len = 4;
+            c.u_min[0] = 0.0f, c.u_max[0] = 0.3f;
+            for(int i = 1; i < 4; ++i) c.u_min[i] = -pi, c.u_max[i] = pi;
+            c.gravity = -0.0981f;
+        }
+    else
+        {
+            set_error("kgmt_config_default: unknown model");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    *out = c;
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_config_validate(const kgmt_config* cfg)
+{
+    RETURN_IF(!cfg, KGMT_ERR_INVALID_ARG, "config is NULL");
+    return validate_config(*cfg);
+}
+
+extern "C" size_t kgmt_query_bytes(const kgmt_config* cfg, uint32_t n_obstacles)
+{
+    if(!cfg || validate_config(*cfg) != KGMT_OK) return 0;
+    return layout_of(*cfg, n_obstacles).total;
+}
+
+static bool is_device_pointer(const void* p)
+{
+    cudaPointerAttributes a;
+    if(cudaPointerGetAttributes(&a, p) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// ---------------------------------------------------------------------------
+// single planner
+// ---------------------------------------------------------------------------
+struct kgmt_planner {
+    Engine eng;
+    DeviceArena arena;
+    kgmt_config cfg;
+    QueryParams params;
+    QueryState state;
+    bool planned = false;
+};
+
+extern "C" kgmt_status kgmt_create(const kgmt_config* cfg, void* stream, kgmt_planner** out)
+{
+    RETURN_IF(!cfg || !out, KGMT_ERR_INVALID_ARG, "kgmt_create: NULL argument");
+    *out = nullptr;
+    CHECK_ST(validate_config(*cfg));
+    kgmt_planner* p = new(std::nothrow) kgmt_planner();
+    RETURN_IF(!p, KGMT_ERR_OOM, "kgmt_create: host allocation failed");
+    p->cfg = *cfg;
+    kgmt_status st = p->eng.init(1, (cudaStream_t)stream, 256, 4, true);
+    if(st == KGMT_OK) st = p->arena.reserve(layout_of(*cfg, 0).total);
+    if(st != KGMT_OK)
+        {
+            delete p;
+            return st;
+        }
+    *out = p;
+    return KGMT_OK;
+}
+
+extern "C" void kgmt_destroy(kgmt_planner* p) { delete p; }
+
+extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                 uint32_t n_obstacles)
+{
+    RETURN_IF(!p || !h_initial || !h_goal, KGMT_ERR_INVALID_ARG, "kgmt_plan: NULL argument");
+    RETURN_IF(n_obstacles > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan: obstacles pointer is NULL");
+    RETURN_IF(n_obstacles > 0 && !is_device_pointer(d_obstacles), KGMT_ERR_INVALID_ARG,
+              "kgmt_plan: obstacles must be a device pointer (as in KGMT::plan)");
+    p->planned = false;
+    const QueryLayout L = layout_of(p->cfg, n_obstacles);
+    p->arena.reset();
+    CHECK_ST(p->arena.reserve(L.total));
+    size_t off = 0;
+    RETURN_IF(!p->arena.alloc(L.total, &off), KGMT_ERR_OOM, "kgmt_plan: arena allocation failed");
+    p->params = make_params(p->cfg, h_initial, h_goal, p->arena.base() + off, L, nullptr, n_obstacles);
+    CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, p->params.obstacles, n_obstacles, p->eng.stream()), "stage obstacles"));
+    p->eng.host_params(0) = p->params;
+    CHECK_ST(p->eng.admit(0, 1, 1));
+    CHECK_ST(p->eng.run_until_done(p->cfg.max_iterations));
+    CHECK_ST(p->eng.extract_paths(1));
+    CHECK_ST(p->eng.read_states(0, 1, &p->state));
+    uint32_t err = 0;
+    CHECK_ST(p->eng.read_error(&err));
+    RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "kgmt_plan: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    p->planned = true;
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_get_result(const kgmt_planner* p, kgmt_result* out)
+{
+    RETURN_IF(!p || !out, KGMT_ERR_INVALID_ARG, "kgmt_get_result: NULL argument");
+    RETURN_IF(!p->planned, KGMT_ERR_NOT_READY, "kgmt_get_result: no plan has completed");
+    *out = to_result(p->state, 0);
+    return KGMT_OK;
+}
+
+static kgmt_status copy_tree_common(const QueryParams& prm, const QueryState& st, cudaStream_t s, float* h_samples, int32_t* h_parents,
+                                    float* h_costs, uint32_t max_nodes)
+{
+    const uint32_t n = st.tree_size < max_nodes ? st.tree_size : max_nodes;
+    const size_t D = prm.sample_dim;
+    if(h_samples) CHECK_ST(cuda_status(cudaMemcpyAsync(h_samples, prm.tree, n * D * 4, cudaMemcpyDeviceToHost, s), "copy tree"));
+    if(h_parents) CHECK_ST(cuda_status(cudaMemcpyAsync(h_parents, prm.parent, n * 4ull, cudaMemcpyDeviceToHost, s), "copy parents"));
+    if(h_costs) CHECK_ST(cuda_status(cudaMemcpyAsync(h_costs, prm.cost, n * 4ull, cudaMemcpyDeviceToHost, s), "copy costs"));
+    return cuda_status(cudaStreamSynchronize(s), "sync");
+}
+
+static kgmt_status copy_path_common(const QueryParams& prm, const QueryState& st, cudaStream_t s, float* h_rows, uint32_t max_rows,
+                                    uint32_t* n_rows)
+{
+    const uint32_t n = st.path_len < max_rows ? st.path_len : max_rows;
+    if(n_rows) *n_rows = n;
+    if(n && h_rows)
+        {
+            CHECK_ST(cuda_status(cudaMemcpyAsync(h_rows, prm.path, (size_t)n * prm.sample_dim * 4, cudaMemcpyDeviceToHost, s), "copy path"));
+            return cuda_status(cudaStreamSynchronize(s), "sync");
+        }
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_copy_tree(kgmt_planner* p, float* h_samples, int32_t* h_parents, float* h_costs, uint32_t max_nodes)
+{
+    RETURN_IF(!p, KGMT_ERR_INVALID_ARG, "kgmt_copy_tree: NULL planner");
+    RETURN_IF(!p->planned, KGMT_ERR_NOT_READY, "kgmt_copy_tree: no plan has completed");
+    return copy_tree_common(p->params, p->state, p->eng.stream(), h_samples, h_parents, h_costs, max_nodes);
+}
+
+extern "C" kgmt_status kgmt_copy_path(kgmt_planner* p, float* h_rows, uint32_t max_rows, uint32_t* n_rows)
+{
+    RETURN_IF(!p, KGMT_ERR_INVALID_ARG, "kgmt_copy_path: NULL planner");
+    RETURN_IF(!p->planned, KGMT_ERR_NOT_READY, "kgmt_copy_path: no plan has completed");
+    return copy_path_common(p->params, p->state, p->eng.stream(), h_rows, max_rows, n_rows);
+}
+
+extern "C" kgmt_status kgmt_device_tree(kgmt_planner* p, const float** d_samples, const int32_t** d_parents, const float** d_costs)
+{
+    RETURN_IF(!p, KGMT_ERR_INVALID_ARG, "kgmt_device_tree: NULL planner");
+    RETURN_IF(!p->planned, KGMT_ERR_NOT_READY, "kgmt_device_tree: no plan has completed");
+    if(d_samples) *d_samples = p->params.tree;
+    if(d_parents) *d_parents = p->params.parent;
+    if(d_costs) *d_costs = p->params.cost;
+    return KGMT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch
+// ---------------------------------------------------------------------------
+struct kgmt_batch {
+    Engine eng;
+    DeviceArena arena;
+    kgmt_batch_options opt;
+    std::vector<QueryState> states;
+    std::vector<QueryParams> params;
+    uint32_t n_last = 0;
+};
+
+extern "C" kgmt_status kgmt_batch_create(const kgmt_batch_options* opt, void* stream, kgmt_batch** out)
+{
+    RETURN_IF(!opt || !out, KGMT_ERR_INVALID_ARG, "kgmt_batch_create: NULL argument");
+    RETURN_IF(opt->max_queries == 0 || opt->max_queries > (1u << 20), KGMT_ERR_INVALID_ARG, "kgmt_batch_create: max_queries");
+    *out = nullptr;
+    kgmt_batch* b = new(std::nothrow) kgmt_batch();
+    RETURN_IF(!b, KGMT_ERR_OOM, "kgmt_batch_create: host allocation failed");
+    b->opt = *opt;
+    kgmt_status st = b->eng.init(opt->max_queries, (cudaStream_t)stream, opt->propagate_block ? opt->propagate_block : 256,
+                                 opt->iters_per_graph ? opt->iters_per_graph : 4, opt->use_graph != 0);
+    if(st != KGMT_OK)
+        {
+            delete b;
+            return st;
+        }
+    *out = b;
+    return KGMT_OK;
+}
+
+extern "C" void kgmt_batch_destroy(kgmt_batch* b) { delete b; }
+
+// lays out n queries + one shared obstacle region + raw staging in the arena
+static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits, const float* h_goals,
+                                 const uint32_t* obs_offset, const uint32_t* obs_count, size_t* raw_off, float4** obs_region,
+                                 uint32_t* n_boxes)
+{
+    RETURN_IF(n == 0 || n > b->eng.slots(), KGMT_ERR_CAPACITY, "batch: query count exceeds max_queries");
+    RETURN_IF(!cfgs || !obs_offset || !obs_count, KGMT_ERR_INVALID_ARG, "batch: NULL argument");
+    uint64_t boxes = 0;
+    uint32_t max_iters = 0;
+    size_t total = 0;
+    std::vector<QueryLayout> L(n);
+    for(uint32_t i = 0; i < n; ++i)
+        {
+            CHECK_ST(validate_config(cfgs[i]));
+            L[i] = layout_of(cfgs[i], 0);
+            total += L[i].total;
+            uint64_t end = (uint64_t)obs_offset[i] + obs_count[i];
+            if(end > boxes) boxes = end;
+            if(cfgs[i].max_iterations > max_iters) max_iters = cfgs[i].max_iterations;
+        }
+    RETURN_IF(boxes > (1ull << 31), KGMT_ERR_INVALID_ARG, "batch: too many obstacles");
+    const size_t obs_bytes = ((boxes * 32 + 255) / 256) * 256;
+    const size_t raw_bytes = ((boxes * 24 + 255) / 256) * 256;
+    b->arena.reset();
+    CHECK_ST(b->arena.reserve(total + obs_bytes + raw_bytes + 4096));
+    size_t obs_off = 0, rawo = 0;
+    RETURN_IF(!b->arena.alloc(obs_bytes ? obs_bytes : 256, &obs_off), KGMT_ERR_OOM, "batch: arena");
+    RETURN_IF(!b->arena.alloc(raw_bytes ? raw_bytes : 256, &rawo), KGMT_ERR_OOM, "batch: arena");
+    float4* region = (float4*)(b->arena.base() + obs_off);
+    b->params.resize(n);
+    for(uint32_t i = 0; i < n; ++i)
+        {
+            size_t off = 0;
+            RETURN_IF(!b->arena.alloc(L[i].total, &off), KGMT_ERR_OOM, "batch: arena");
+            const float* init = h_inits ? h_inits + (size_t)i * KGMT_MAX_SAMPLE_DIM : nullptr;
+            const float* goal = h_goals ? h_goals + (size_t)i * KGMT_MAX_SAMPLE_DIM : nullptr;
+            b->params[i] = make_params(cfgs[i], init, goal, b->arena.base() + off, L[i], region + 2 * (size_t)obs_offset[i], obs_count[i]);
+            b->eng.host_params(i) = b->params[i];
+        }
+    *raw_off = rawo;
+    *obs_region = region;
+    *n_boxes = (uint32_t)boxes;
+    return KGMT_OK;
+}
+
+static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* d_inits, const float* d_goals,
+                             kgmt_result* results)
+{
+    uint32_t max_iters = 0;
+    for(uint32_t i = 0; i < n; ++i)
+        if(cfgs[i].max_iterations > max_iters) max_iters = cfgs[i].max_iterations;
+    CHECK_ST(b->eng.admit(0, n, n, d_inits, d_goals));
+    CHECK_ST(b->eng.run_until_done(max_iters));
+    CHECK_ST(b->eng.extract_paths(n));
+    b->states.resize(n);
+    CHECK_ST(b->eng.read_states(0, n, b->states.data()));
+    uint32_t err = 0;
+    CHECK_ST(b->eng.read_error(&err));
+    b->n_last = n;
+    RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "batch: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    if(results)
+        for(uint32_t i = 0; i < n; ++i) results[i] = to_result(b->states[i], i);
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_plan_batch(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits, const float* h_goals,
+                                       const float* h_obstacles, const uint32_t* obs_offset, const uint32_t* obs_count,
+                                       kgmt_result* results)
+{
+    RETURN_IF(!b || !h_inits || !h_goals, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch: NULL argument");
+    b->n_last = 0;
+    size_t raw_off = 0;
+    float4* region = nullptr;
+    uint32_t boxes = 0;
+    CHECK_ST(batch_prepare(b, n, cfgs, h_inits, h_goals, obs_offset, obs_count, &raw_off, &region, &boxes));
+    RETURN_IF(boxes > 0 && !h_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch: obstacles pointer is NULL");
+    cudaStream_t s = b->eng.stream();
+    float* raw = (float*)(b->arena.base() + raw_off);
+    if(boxes)
+        {
+            CHECK_ST(cuda_status(cudaMemcpyAsync(raw, h_obstacles, (size_t)boxes * 24, cudaMemcpyHostToDevice, s), "upload obstacles"));
+            CHECK_ST(cuda_status(launch_stage_obstacles(raw, region, boxes, s), "stage obstacles"));
+        }
+    return batch_run(b, n, cfgs, nullptr, nullptr, results);
+}
+
+extern "C" kgmt_status kgmt_plan_batch_device(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* d_inits,
+                                              const float* d_goals, const float* d_obstacles, const uint32_t* h_obs_offset,
+                                              const uint32_t* h_obs_count, kgmt_result* results)
+{
+    RETURN_IF(!b || !d_inits || !d_goals, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch_device: NULL argument");
+    b->n_last = 0;
+    size_t raw_off = 0;
+    float4* region = nullptr;
+    uint32_t boxes = 0;
+    CHECK_ST(batch_prepare(b, n, cfgs, nullptr, nullptr, h_obs_offset, h_obs_count, &raw_off, &region, &boxes));
+    RETURN_IF(boxes > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch_device: obstacles pointer is NULL");
+    if(boxes) CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, region, boxes, b->eng.stream()), "stage obstacles"));
+    return batch_run(b, n, cfgs, d_inits, d_goals, results);
+}
+
+extern "C" kgmt_status kgmt_batch_copy_tree(kgmt_batch* b, uint32_t i, float* h_samples, int32_t* h_parents, float* h_costs,
+                                            uint32_t max_nodes)
+{
+    RETURN_IF(!b, KGMT_ERR_INVALID_ARG, "kgmt_batch_copy_tree: NULL batch");
+    RETURN_IF(i >= b->n_last, KGMT_ERR_NOT_READY, "kgmt_batch_copy_tree: no such query in the last batch");
+    return copy_tree_common(b->params[i], b->states[i], b->eng.stream(), h_samples, h_parents, h_costs, max_nodes);
+}
+
+extern "C" kgmt_status kgmt_batch_copy_path(kgmt_batch* b, uint32_t i, float* h_rows, uint32_t max_rows, uint32_t* n_rows)
+{
+    RETURN_IF(!b, KGMT_ERR_INVALID_ARG, "kgmt_batch_copy_path: NULL batch");
+    RETURN_IF(i >= b->n_last, KGMT_ERR_NOT_READY, "kgmt_batch_copy_path: no such query in the last batch");
+    return copy_path_common(b->params[i], b->states[i], b->eng.stream(), h_rows, max_rows, n_rows);
+}
+
+extern "C" kgmt_status kgmt_batch_autotune(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits, const float* h_goals,
+                                           const float* h_obstacles, const uint32_t* obs_offset, const uint32_t* obs_count,
+                                           uint32_t* best_block)
+{
+    RETURN_IF(!b, KGMT_ERR_INVALID_ARG, "kgmt_batch_autotune: NULL batch");
+    const uint32_t blocks[4] = {64, 128, 256, 512};
+    double best_t = 1e30;
+    uint32_t best = b->eng.prop_block();
+    for(uint32_t blk : blocks)
+        {
+            CHECK_ST(b->eng.set_prop_block(blk));
+            // one warm-up, then the timed run
+            CHECK_ST(kgmt_plan_batch(b, n, cfgs, h_inits, h_goals, h_obstacles, obs_offset, obs_count, nullptr));
+            auto t0 = std::chrono::steady_clock::now();
+            CHECK_ST(kgmt_plan_batch(b, n, cfgs, h_inits, h_goals, h_obstacles, obs_offset, obs_count, nullptr));
+            double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if(t < best_t)
+                {
+                    best_t = t;
+                    best = blk;
+                }
+        }
+    CHECK_ST(b->eng.set_prop_block(best));
+    if(best_block) *best_block = best;
+    return KGMT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// server: continuous batching with memory-based admission
+// ---------------------------------------------------------------------------
+struct PendingQuery {
+    uint64_t ticket;
+    kgmt_config cfg;
+    float init[KGMT_MAX_SAMPLE_DIM];
+    float goal[KGMT_MAX_SAMPLE_DIM];
+    std::vector<float> obstacles;
+    std::chrono::steady_clock::time_point submitted;
+};
+
+struct ResidentQuery {
+    bool used = false;
+    uint64_t ticket = 0;
+    size_t offset = 0;
+    std::chrono::steady_clock::time_point submitted;
+};
+
+struct kgmt_server {
+    Engine eng;
+    DeviceArena arena;
+    kgmt_server_options opt;
+    std::deque<PendingQuery> queue;
+    std::vector<ResidentQuery> slots;
+    std::deque<kgmt_result> done;
+    std::vector<QueryState> states;
+    uint64_t next_ticket = 1;
+    uint32_t running = 0;
+};
+
+extern "C" kgmt_status kgmt_server_create(const kgmt_server_options* opt, void* stream, kgmt_server** out)
+{
+    RETURN_IF(!opt || !out, KGMT_ERR_INVALID_ARG, "kgmt_server_create: NULL argument");
+    RETURN_IF(opt->max_slots == 0 || opt->max_slots > (1u << 16), KGMT_ERR_INVALID_ARG, "kgmt_server_create: max_slots");
+    RETURN_IF(opt->memory_budget < (1ull << 20), KGMT_ERR_INVALID_ARG, "kgmt_server_create: memory_budget below 1 MiB");
+    *out = nullptr;
+    kgmt_server* s = new(std::nothrow) kgmt_server();
+    RETURN_IF(!s, KGMT_ERR_OOM, "kgmt_server_create: host allocation failed");
+    s->opt = *opt;
+    if(s->opt.iters_per_step == 0) s->opt.iters_per_step = 1;
+    kgmt_status st = s->eng.init(opt->max_slots, (cudaStream_t)stream, opt->propagate_block ? opt->propagate_block : 256, 1, false);
+    if(st == KGMT_OK) st = s->arena.reserve(opt->memory_budget);
+    if(st == KGMT_OK) st = s->eng.set_active(opt->max_slots);
+    if(st != KGMT_OK)
+        {
+            delete s;
+            return st;
+        }
+    s->slots.resize(opt->max_slots);
+    s->states.resize(opt->max_slots);
+    *out = s;
+    return KGMT_OK;
+}
+
+extern "C" void kgmt_server_destroy(kgmt_server* s) { delete s; }
+
+extern "C" kgmt_status kgmt_server_submit(kgmt_server* s, const kgmt_config* cfg, const float* h_init, const float* h_goal,
+                                          const float* h_obstacles, uint32_t n_obstacles, uint64_t* ticket)
+{
+    RETURN_IF(!s || !cfg || !h_init || !h_goal, KGMT_ERR_INVALID_ARG, "kgmt_server_submit: NULL argument");
+    RETURN_IF(n_obstacles > 0 && !h_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_server_submit: obstacles pointer is NULL");
+    CHECK_ST(validate_config(*cfg));
+    const QueryLayout L = layout_of(*cfg, n_obstacles);
+    RETURN_IF(L.total + (size_t)n_obstacles * 24 + 256 > s->arena.capacity(), KGMT_ERR_OOM,
+              "kgmt_server_submit: query larger than the memory budget");
+    PendingQuery q;
+    q.ticket = s->next_ticket++;
+    q.cfg = *cfg;
+    const uint32_t D = sample_dim_of(cfg->model);
+    std::memset(q.init, 0, sizeof(q.init));
+    std::memset(q.goal, 0, sizeof(q.goal));
+    std::memcpy(q.init, h_init, D * sizeof(float));
+    std::memcpy(q.goal, h_goal, 3 * sizeof(float));
+    q.obstacles.assign(h_obstacles, h_obstacles + (size_t)n_obstacles * 6);
+    q.submitted = std::chrono::steady_clock::now();
+    s->queue.push_back(std::move(q));
+    if(ticket) *ticket = s->queue.back().ticket;
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uint32_t* n_queued)
+{
+    RETURN_IF(!s, KGMT_ERR_INVALID_ARG, "kgmt_server_step: NULL server");
+    cudaStream_t st = s->eng.stream();
+    // ---- admission: FIFO while a slot and memory are free ----
+    bool admitted = false;
+    uint32_t slot = 0;
+    while(!s->queue.empty())
+        {
+            while(slot < s->slots.size() && s->slots[slot].used) ++slot;
+            if(slot >= s->slots.size()) break;
+            PendingQuery& q = s->queue.front();
+            const uint32_t n_obs = (uint32_t)(q.obstacles.size() / 6);
+            const QueryLayout L = layout_of(q.cfg, n_obs);
+            const size_t raw_at = (L.total + 255) & ~size_t(255);
+            size_t off = 0;
+            if(!s->arena.alloc(raw_at + (size_t)n_obs * 24 + 256, &off)) break;  // wait for memory
+            char* chunk = s->arena.base() + off;
+            QueryParams prm = make_params(q.cfg, q.init, q.goal, chunk, L, nullptr, n_obs);
+            if(n_obs)
+                {
+                    float* raw = (float*)(chunk + raw_at);
+                    CHECK_ST(cuda_status(cudaMemcpyAsync(raw, q.obstacles.data(), (size_t)n_obs * 24, cudaMemcpyHostToDevice, st),
+                                         "upload obstacles"));
+                    CHECK_ST(cuda_status(launch_stage_obstacles(raw, prm.obstacles, n_obs, st), "stage obstacles"));
+                }
+            s->eng.host_params(slot) = prm;
+            CHECK_ST(s->eng.upload_params(slot, 1));
+            CHECK_ST(s->eng.init_slots(slot, 1));
+            ResidentQuery& r = s->slots[slot];
+            r.used = true;
+            r.ticket = q.ticket;
+            r.offset = off;
+            r.submitted = q.submitted;
+            s->queue.pop_front();
+            admitted = true;
+            ++s->running;
+        }
+    if(admitted) CHECK_ST(s->eng.schedule());
+    // ---- iterations for every resident query ----
+    if(s->running) CHECK_ST(s->eng.run_iterations(s->opt.iters_per_step));
+    // ---- retire finished queries ----
+    const uint32_t n = (uint32_t)s->slots.size();
+    CHECK_ST(s->eng.read_states(0, n, s->states.data()));
+    const auto now = std::chrono::steady_clock::now();
+    uint32_t running = 0;
+    for(uint32_t i = 0; i < n; ++i)
+        {
+            ResidentQuery& r = s->slots[i];
+            if(!r.used) continue;
+            const QueryState& qs = s->states[i];
+            if(qs.status == KGMT_QUERY_RUNNING)
+                {
+                    ++running;
+                    continue;
+                }
+            kgmt_result res = to_result(qs, r.ticket);
+            res.latency_ms = (float)(std::chrono::duration<double, std::milli>(now - r.submitted).count());
+            s->done.push_back(res);
+            s->arena.release(r.offset);
+            r.used = false;
+        }
+    s->running = running;
+    uint32_t err = 0;
+    CHECK_ST(s->eng.read_error(&err));
+    RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "server: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    if(n_running) *n_running = running;
+    if(n_queued) *n_queued = (uint32_t)s->queue.size();
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_server_poll(kgmt_server* s, kgmt_result* out, uint32_t max, uint32_t* n_out)
+{
+    RETURN_IF(!s || (!out && max > 0), KGMT_ERR_INVALID_ARG, "kgmt_server_poll: NULL argument");
+    uint32_t k = 0;
+    while(k < max && !s->done.empty())
+        {
+            out[k++] = s->done.front();
+            s->done.pop_front();
+        }
+    if(n_out) *n_out = k;
+    return KGMT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// function-level propagation
+// ---------------------------------------------------------------------------
+extern "C" kgmt_status kgmt_propagate_samples(const kgmt_config* cfg, const float* d_x0, const float* d_uniforms, const float* d_obstacles,
+                                              uint32_t n_obstacles, uint32_t n, float* d_x1, uint8_t* d_valid, int32_t* d_r1, int32_t* d_r2,
+                                              void* stream)
+{
+    RETURN_IF(!cfg || (n > 0 && (!d_x0 || !d_uniforms || !d_x1 || !d_valid)), KGMT_ERR_INVALID_ARG, "kgmt_propagate_samples: NULL argument");
+    RETURN_IF(n_obstacles > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_propagate_samples: obstacles pointer is NULL");
+    RETURN_IF(n_obstacles > 6000, KGMT_ERR_INVALID_ARG, "kgmt_propagate_samples: at most 6000 obstacles");
+    CHECK_ST(validate_config(*cfg));
+    int dev_count = 0;
+    if(cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+        {
+            cudaGetLastError();
+            set_error("no CUDA device");
+            return KGMT_ERR_NO_DEVICE;
+        }
+    const QueryLayout L = layout_of(*cfg, 0);
+    QueryParams p = make_params(*cfg, nullptr, nullptr, nullptr, L, nullptr, n_obstacles);
+    return cuda_status(
+      launch_propagate_samples(p, d_x0, d_uniforms, d_obstacles, n_obstacles, n, d_x1, d_valid, d_r1, d_r2, (cudaStream_t)stream),
+      "k_propagate_samples");
+}

@@ -1,0 +1,297 @@
+// kgmt_device.cuh -- per-sample device math of the KGMT planning loop.
+//
+// Everything here is compiled with -fmad=false: every float multiply and add
+// is rounded on its own, in the order written, so the region ids, collision
+// verdicts, acceptance decisions and therefore the whole tree are
+// reproducible bit for bit by a single-precision CPU restatement that keeps
+// the same order (-ffp-contract=off).
+//
+// Reference counterparts (nipe1783/KGMT):
+//   Philox sampling replaces curand XORWOW   src/planners/Planner.cu:37-50
+//   double integrator                        src/statePropagator/statePropagator.cu:76-142
+//   quadrotor RK4 + ode                      src/statePropagator/statePropagator.cu:246-370
+//   swept AABB broad phase                   src/collisionCheck/collisionCheck.cu:3-10, 49-61
+//   coarse / fine region ids                 src/graphs/Graph.cu:99-153, 155-205
+//   goal distance                            include/helper/helper.cuh:138-152
+#pragma once
+#include <cstdint>
+
+#include "kgmt_types.h"
+
+namespace kgmt {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Counter (index, itr,
+// domain, block), key = 64-bit query seed.
+// ---------------------------------------------------------------------------
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for(int r = 0; r < 10; ++r)
+        {
+            uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+            uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+            uint32_t n0 = hi1 ^ c1 ^ k0;
+            uint32_t n2 = hi0 ^ c3 ^ k1;
+            c0 = n0;
+            c1 = lo1;
+            c2 = n2;
+            c3 = lo0;
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+    return {c0, c1, c2, c3};
+}
+
+// uniform in (0, 1], like curand_uniform
+__device__ __forceinline__ float u01(uint32_t x) { return (float)((x >> 8) + 1u) * 0x1.0p-24f; }
+
+// ---------------------------------------------------------------------------
+// Portable sine/cosine: Cody & Waite reduction by pi/2 (three-part split,
+// n*P1 and n*P2 exact for |n| < 2^13) and Taylor polynomials (degree 9 / 10)
+// on |r| <= pi/4, Horner form, coefficients 1/n! rounded to float.  Written
+// from the series so the CPU restatement rounds identically; accuracy about
+// one ulp for |x| < 1e4.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
+{
+    float n = rintf(x * 0x1.45f306p-1f);
+    float r = ((x - n * 0x1.92p+0f) - n * 0x1.fb4p-12f) - n * 0x1.4442d2p-24f;
+    float qf = n - 4.0f * floorf(n * 0.25f);
+    int q = (qf >= 0.0f && qf <= 3.0f) ? (int)qf : 0;
+    float r2 = r * r;
+    float sp = r + (r * r2) * (-0x1.555556p-3f + r2 * (0x1.111112p-7f + r2 * (-0x1.a01a02p-13f + r2 * 0x1.71de3ap-19f)));
+    float cp = 1.0f + r2 * (-0x1.0p-1f + r2 * (0x1.555556p-5f + r2 * (-0x1.6c16c2p-10f + r2 * (0x1.a01a02p-16f + r2 * -0x1.27e4fcp-22f))));
+    float ss = (q & 1) ? cp : sp;
+    float cc = (q & 1) ? sp : cp;
+    s = (q == 2 || q == 3) ? -ss : ss;
+    c = (q == 1 || q == 2) ? -cc : cc;
+}
+
+// ---------------------------------------------------------------------------
+// Regions on workspace-only grids.  r1 = (ix*L + iy)*L + iz (z least
+// significant, Graph.cu:105-113); the fine cell is located relative to the
+// exact corner ws_min + idx * cell_size.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cell_index(float t, int len)
+{
+    if(!(t >= 0.0f)) return 0;
+    if(t >= (float)len) return len - 1;
+    int i = (int)t;
+    return i > len - 1 ? len - 1 : i;
+}
+
+struct CellIds {
+    int r1;
+    int r2;  // fine cell inside r1, [0, fine_len^3)
+};
+
+__device__ __forceinline__ CellIds cell_ids(const QueryParams& P, float x, float y, float z)
+{
+    const float Lf = (float)P.coarse_len;
+    const int L = (int)P.coarse_len;
+    int ix = cell_index((Lf * (x - P.ws_min)) / P.ws_range, L);
+    int iy = cell_index((Lf * (y - P.ws_min)) / P.ws_range, L);
+    int iz = cell_index((Lf * (z - P.ws_min)) / P.ws_range, L);
+    const float Ff = (float)P.fine_len;
+    const int F = (int)P.fine_len;
+    float mx = P.ws_min + (float)ix * P.cell_size;
+    float my = P.ws_min + (float)iy * P.cell_size;
+    float mz = P.ws_min + (float)iz * P.cell_size;
+    int jx = cell_index((Ff * (x - mx)) / P.cell_size, F);
+    int jy = cell_index((Ff * (y - my)) / P.cell_size, F);
+    int jz = cell_index((Ff * (z - mz)) / P.cell_size, F);
+    return {(ix * L + iy) * L + iz, (jx * F + jy) * F + jz};
+}
+
+__device__ __forceinline__ int region_of(const QueryParams& P, float x, float y, float z)
+{
+    const float Lf = (float)P.coarse_len;
+    const int L = (int)P.coarse_len;
+    int ix = cell_index((Lf * (x - P.ws_min)) / P.ws_range, L);
+    int iy = cell_index((Lf * (y - P.ws_min)) / P.ws_range, L);
+    int iz = cell_index((Lf * (z - P.ws_min)) / P.ws_range, L);
+    return (ix * L + iy) * L + iz;
+}
+
+__device__ __forceinline__ float goal_distance(float x, float y, float z, const QueryParams& P)
+{
+    float dx = x - P.goal[0], dy = y - P.goal[1], dz = z - P.goal[2];
+    float s = (dx * dx + dy * dy) + dz * dz;
+    return sqrtf(s);
+}
+
+// ---------------------------------------------------------------------------
+// Swept-AABB broad phase against boxes stored as two float4 (min.xyz, max.xyz).
+// Separated iff bbMax <= obsMin or obsMax <= bbMin on some axis; touching is
+// free.  Returns true when the step box hits no obstacle.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool step_free(const float4* __restrict__ obs, uint32_t n_obs, float ax, float ay, float az, float bx,
+                                          float by, float bz)
+{
+    const float lx = ax > bx ? bx : ax, hx = ax > bx ? ax : bx;
+    const float ly = ay > by ? by : ay, hy = ay > by ? ay : by;
+    const float lz = az > bz ? bz : az, hz = az > bz ? az : bz;
+    bool hit = false;
+    for(uint32_t o = 0; o < n_obs; ++o)
+        {
+            const float4 mn = obs[2 * o];
+            const float4 mx = obs[2 * o + 1];
+            const bool sep = (hx <= mn.x) | (mx.x <= lx) | (hy <= mn.y) | (mx.y <= ly) | (hz <= mn.z) | (mx.z <= lz);
+            hit |= !sep;
+        }
+    return !hit;
+}
+
+// ---------------------------------------------------------------------------
+// Controls and step count (statePropagator.cu:78-81 / 248-253).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int draw_steps(const QueryParams& P, float u)
+{
+    int k = (int)P.min_steps + (int)(u * P.step_span);
+    return k > (int)P.max_steps ? (int)P.max_steps : k;
+}
+
+// ---------------------------------------------------------------------------
+// Double integrator.  `rule` selects the classic RK4 position update or the
+// reference's own formula (statePropagator.cu:97-99, (5v + 2ah) h / 6).
+// x0/x1 are sample rows [x y z vx vy vz ax ay az duration].
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
+                                             float* x1)
+{
+    const float a0 = P.u_min[0] + u[0] * P.u_span[0];
+    const float a1 = P.u_min[1] + u[1] * P.u_span[1];
+    const float a2 = P.u_min[2] + u[2] * P.u_span[2];
+    const int k = draw_steps(P, u[3]);
+    const float h = P.step_size;
+    float p[3] = {x0[0], x0[1], x0[2]};
+    float v[3] = {x0[3], x0[4], x0[5]};
+    const float a[3] = {a0, a1, a2};
+    const bool ref_rule = P.di_rule == KGMT_DI_RULE_REFERENCE;
+    bool ok = true;
+    for(int i = 0; i < k; ++i)
+        {
+            const float q0 = p[0], q1 = p[1], q2 = p[2];
+#pragma unroll
+            for(int d = 0; d < 3; ++d)
+                {
+                    float half = v[d] + (a[d] * h) / 2.0f;
+                    float full = v[d] + a[d] * h;
+                    float sum = ref_rule ? v[d] + ((v[d] + 2.0f * half) + full) : ((v[d] + 2.0f * half) + 2.0f * half) + full;
+                    p[d] = p[d] + (sum * h) / 6.0f;
+                }
+#pragma unroll
+            for(int d = 0; d < 3; ++d) v[d] = v[d] + ((((a[d] + 2.0f * a[d]) + 2.0f * a[d]) + a[d]) * h) / 6.0f;
+            if(v[0] < P.v_min || v[0] > P.v_max || v[1] < P.v_min || v[1] > P.v_max || v[2] < P.v_min || v[2] > P.v_max)
+                {
+                    ok = false;
+                    break;
+                }
+            if(p[0] < P.ws_min || p[0] > P.ws_max || p[1] < P.ws_min || p[1] > P.ws_max || p[2] < P.ws_min || p[2] > P.ws_max)
+                {
+                    ok = false;
+                    break;
+                }
+            if(!step_free(obs, n_obs, q0, q1, q2, p[0], p[1], p[2]))
+                {
+                    ok = false;
+                    break;
+                }
+        }
+    x1[0] = p[0], x1[1] = p[1], x1[2] = p[2];
+    x1[3] = v[0], x1[4] = v[1], x1[5] = v[2];
+    x1[6] = a0, x1[7] = a1, x1[8] = a2;
+    x1[9] = h * (float)k;
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// 12-D quadrotor: state [x y z phi theta psi u v w p q r], controls
+// [Zc Lc Mc Nc], classic RK4 over the rigid-body ode of
+// statePropagator.cu:325-370 (Euler-angle kinematics, drag -nu|v|, -mu|w|).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, float zc, float lc, float mc, float nc, float* d)
+{
+    const float phi = s[3], theta = s[4], psi = s[5];
+    const float uu = s[6], vv = s[7], ww = s[8];
+    const float p = s[9], q = s[10], r = s[11];
+    float sphi, cphi, sth, cth, spsi, cpsi;
+    sincos_portable(phi, sphi, cphi);
+    sincos_portable(theta, sth, cth);
+    sincos_portable(psi, spsi, cpsi);
+    const float tth = sth / cth;
+    d[0] = ((cth * cpsi) * uu + ((sphi * sth) * cpsi - cphi * spsi) * vv) + ((cphi * sth) * cpsi + sphi * spsi) * ww;
+    d[1] = ((cth * spsi) * uu + ((sphi * sth) * spsi + cphi * cpsi) * vv) + ((cphi * sth) * spsi - sphi * cpsi) * ww;
+    d[2] = ((-sth) * uu + (sphi * cth) * vv) + (cphi * cth) * ww;
+    const float qr = q * sphi + r * cphi;
+    d[3] = p + qr * tth;
+    d[4] = q * cphi - r * sphi;
+    d[5] = qr / cth;
+    const float xyz = (-P.nu) * sqrtf((uu * uu + vv * vv) + ww * ww);
+    const float mx = P.mass_inv * xyz;
+    d[6] = ((r * vv - q * ww) - P.gravity * sth) + mx * uu;
+    d[7] = ((p * ww - r * uu) + (P.gravity * cth) * sphi) + mx * vv;
+    d[8] = (((q * uu - p * vv) + (P.gravity * cth) * cphi) + mx * ww) + P.mass_inv * zc;
+    const float lmn = (-P.mu) * sqrtf((p * p + q * q) + r * r);
+    d[9] = ((P.jx * q) * r + (P.iix * lmn) * p) + P.iix * lc;
+    d[10] = ((P.jy * p) * r + (P.iiy * lmn) * q) + P.iiy * mc;
+    d[11] = ((P.jz * p) * q + (P.iiz * lmn) * r) + P.iiz * nc;
+}
+
+__device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
+                                               float* x1)
+{
+    const float zc = P.u_min[0] + u[0] * P.u_span[0];
+    const float lc = P.u_min[1] + u[1] * P.u_span[1];
+    const float mc = P.u_min[2] + u[2] * P.u_span[2];
+    const float nc = P.u_min[3] + u[3] * P.u_span[3];
+    const int k = draw_steps(P, u[4]);
+    const float h = P.step_size, hh = P.half_step, h6 = P.sixth_step;
+    float s[12], k1[12], k2[12], k3[12], k4[12], t[12];
+#pragma unroll
+    for(int j = 0; j < 12; ++j) s[j] = x0[j];
+    bool ok = true;
+    for(int i = 0; i < k; ++i)
+        {
+            const float q0 = s[0], q1 = s[1], q2 = s[2];
+            quad_ode(P, s, zc, lc, mc, nc, k1);
+#pragma unroll
+            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k1[j];
+            quad_ode(P, t, zc, lc, mc, nc, k2);
+#pragma unroll
+            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k2[j];
+            quad_ode(P, t, zc, lc, mc, nc, k3);
+#pragma unroll
+            for(int j = 0; j < 12; ++j) t[j] = s[j] + h * k3[j];
+            quad_ode(P, t, zc, lc, mc, nc, k4);
+#pragma unroll
+            for(int j = 0; j < 12; ++j) s[j] = s[j] + h6 * (((k1[j] + 2.0f * k2[j]) + 2.0f * k3[j]) + k4[j]);
+            if(s[6] < P.v_min || s[6] > P.v_max || s[7] < P.v_min || s[7] > P.v_max || s[8] < P.v_min || s[8] > P.v_max)
+                {
+                    ok = false;
+                    break;
+                }
+            if(s[0] < P.ws_min || s[0] > P.ws_max || s[1] < P.ws_min || s[1] > P.ws_max || s[2] < P.ws_min || s[2] > P.ws_max)
+                {
+                    ok = false;
+                    break;
+                }
+            if(!step_free(obs, n_obs, q0, q1, q2, s[0], s[1], s[2]))
+                {
+                    ok = false;
+                    break;
+                }
+        }
+#pragma unroll
+    for(int j = 0; j < 12; ++j) x1[j] = s[j];
+    x1[12] = zc, x1[13] = lc, x1[14] = mc, x1[15] = nc;
+    x1[16] = h * (float)k;
+    return ok;
+}
+
+}  // namespace kgmt

@@ -1,0 +1,537 @@
+// kgmt_engine.cu -- host runtime: device arena, per-query layout, parameter
+// derivation and the iteration loop (direct launches or CUDA-graph replay).
+//
+// Reference counterparts: buffer construction of Planner::Planner / KGMT::KGMT
+// (src/planners/Planner.cu:4-35, src/planners/KGMT.cu:4-39, Graph::Graph
+// src/graphs/Graph.cu:5-42) and the host loop of KGMT::plan
+// (src/planners/KGMT.cu:84-95), which read sizes back from the device about
+// six times per iteration; here the schedule stays on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "kgmt_engine.h"
+
+namespace kgmt {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+kgmt_status cuda_status(cudaError_t e, const char* what)
+{
+    if(e == cudaSuccess) return KGMT_OK;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    if(e == cudaErrorMemoryAllocation) return KGMT_ERR_OOM;
+    if(e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return KGMT_ERR_NO_DEVICE;
+    return KGMT_ERR_CUDA;
+}
+
+#define KGMT_CUDA(call, what)                                 \
+    do {                                                      \
+        kgmt_status st_ = cuda_status((call), what);          \
+        if(st_ != KGMT_OK) return st_;                        \
+    } while(0)
+
+// ---------------------------------------------------------------------------
+// arena
+// ---------------------------------------------------------------------------
+DeviceArena::~DeviceArena()
+{
+    if(base_) cudaFree(base_);
+}
+
+kgmt_status DeviceArena::reserve(size_t bytes)
+{
+    if(bytes <= cap_) return KGMT_OK;
+    if(!used_.empty())
+        {
+            set_error("arena: cannot grow while allocations are live");
+            return KGMT_ERR_INTERNAL;
+        }
+    if(base_) cudaFree(base_);
+    base_ = nullptr;
+    cap_ = 0;
+    free_.clear();
+    bytes = (bytes + 4095) & ~size_t(4095);
+    KGMT_CUDA(cudaMalloc(&base_, bytes), "cudaMalloc(arena)");
+    cap_ = bytes;
+    free_[0] = bytes;
+    used_bytes_ = 0;
+    return KGMT_OK;
+}
+
+bool DeviceArena::alloc(size_t bytes, size_t* offset)
+{
+    bytes = (bytes + 255) & ~size_t(255);
+    for(auto it = free_.begin(); it != free_.end(); ++it)
+        {
+            if(it->second >= bytes)
+                {
+                    size_t off = it->first, sz = it->second;
+                    free_.erase(it);
+                    if(sz > bytes) free_[off + bytes] = sz - bytes;
+                    used_[off] = bytes;
+                    used_bytes_ += bytes;
+                    *offset = off;
+                    return true;
+                }
+        }
+    return false;
+}
+
+void DeviceArena::release(size_t offset)
+{
+    auto it = used_.find(offset);
+    if(it == used_.end()) return;
+    size_t sz = it->second;
+    used_.erase(it);
+    used_bytes_ -= sz;
+    auto nx = free_.lower_bound(offset);
+    if(nx != free_.end() && offset + sz == nx->first)
+        {
+            sz += nx->second;
+            nx = free_.erase(nx);
+        }
+    if(nx != free_.begin())
+        {
+            auto pv = std::prev(nx);
+            if(pv->first + pv->second == offset)
+                {
+                    pv->second += sz;
+                    return;
+                }
+        }
+    free_[offset] = sz;
+}
+
+void DeviceArena::reset()
+{
+    used_.clear();
+    free_.clear();
+    used_bytes_ = 0;
+    if(cap_) free_[0] = cap_;
+}
+
+// ---------------------------------------------------------------------------
+// layout / params
+// ---------------------------------------------------------------------------
+uint32_t sample_dim_of(int32_t model) { return model == KGMT_MODEL_QUADROTOR ? 17u : 10u; }
+
+kgmt_status validate_config(const kgmt_config& c)
+{
+    auto bad = [](const char* m) {
+        set_error(std::string("invalid config: ") + m);
+        return KGMT_ERR_INVALID_ARG;
+    };
+    if(c.model != KGMT_MODEL_DOUBLE_INTEGRATOR && c.model != KGMT_MODEL_QUADROTOR) return bad("model");
+    if(c.di_rule != KGMT_DI_RULE_RK4 && c.di_rule != KGMT_DI_RULE_REFERENCE) return bad("di_rule");
+    if(c.tree_capacity < 2 || c.tree_capacity > (1u << 28)) return bad("tree_capacity must be in [2, 2^28]");
+    if(c.samples_per_node < 1 || c.samples_per_node > 1024) return bad("samples_per_node must be in [1, 1024]");
+    if(c.max_iterations < 1 || c.max_iterations > 100000) return bad("max_iterations must be in [1, 100000]");
+    if(c.min_steps < 1 || c.min_steps > c.max_steps || c.max_steps > 10000) return bad("need 1 <= min_steps <= max_steps <= 10000");
+    if(!(c.step_size > 0.0f) || !std::isfinite(c.step_size)) return bad("step_size");
+    if(!(c.ws_max > c.ws_min)) return bad("ws_max must exceed ws_min");
+    if(c.coarse_len < 1 || c.coarse_len > 128) return bad("coarse_len must be in [1, 128]");
+    if(c.fine_len < 1 || c.fine_len * c.fine_len * c.fine_len > KGMT_MAX_FINE_CELLS) return bad("fine_len^3 must be in [1, 64]");
+    if(!(c.v_max >= c.v_min)) return bad("v_max < v_min");
+    if(!(c.goal_radius >= 0.0f) || !(c.epsilon >= 0.0f)) return bad("goal_radius / epsilon");
+    if(c.model == KGMT_MODEL_QUADROTOR && (c.ix == 0.0f || c.iy == 0.0f || c.iz == 0.0f)) return bad("inertia must be non-zero");
+    return KGMT_OK;
+}
+
+static size_t aligned(size_t& cur, size_t bytes)
+{
+    size_t off = cur;
+    cur += (bytes + 255) & ~size_t(255);
+    return off;
+}
+
+QueryLayout layout_of(const kgmt_config& c, uint32_t inline_obstacles)
+{
+    QueryLayout L{};
+    const size_t T = c.tree_capacity, D = sample_dim_of(c.model);
+    const size_t R1 = (size_t)c.coarse_len * c.coarse_len * c.coarse_len;
+    L.tiles_per_chain = (uint32_t)((T + kTileC - 1) / kTileC + 1);
+    size_t cur = 0;
+    L.tree = aligned(cur, T * D * 4);
+    L.parent = aligned(cur, T * 4);
+    L.cost = aligned(cur, T * 4);
+    L.node_r1 = aligned(cur, T * 4);
+    L.rep_old = aligned(cur, T * 4);
+    L.rep_new = aligned(cur, T * 4);
+    L.us = aligned(cur, T * D * 4);
+    L.up = aligned(cur, T * 4);
+    L.ur1 = aligned(cur, T * 4);
+    L.uflag = aligned(cur, T);
+    L.counter = aligned(cur, R1 * 4);
+    L.valid = aligned(cur, R1 * 4);
+    L.score = aligned(cur, R1 * 4);
+    L.marks = aligned(cur, R1 * 8);
+    L.newmarks = aligned(cur, R1 * 8);
+    L.tiles_old = aligned(cur, (size_t)L.tiles_per_chain * 8);
+    L.tiles_slot = aligned(cur, (size_t)L.tiles_per_chain * 8);
+    L.path = aligned(cur, ((size_t)c.max_iterations + 2) * D * 4);
+    L.obstacles = aligned(cur, (size_t)inline_obstacles * 32);
+    L.total = cur;
+    return L;
+}
+
+QueryParams make_params(const kgmt_config& c, const float* init, const float* goal, char* chunk, const QueryLayout& L, float4* obstacles,
+                        uint32_t n_obstacles)
+{
+    QueryParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.model = c.model;
+    p.di_rule = c.di_rule;
+    p.capacity = c.tree_capacity;
+    p.samples_per_node = c.samples_per_node;
+    p.max_iterations = c.max_iterations;
+    p.min_steps = c.min_steps;
+    p.max_steps = c.max_steps;
+    p.sample_dim = sample_dim_of(c.model);
+    // derived values in float, the same operations the CPU restatement uses
+    volatile float h = c.step_size;
+    p.step_span = (float)(c.max_steps - c.min_steps + 1u);
+    p.step_size = h;
+    p.half_step = 0.5f * h;
+    p.sixth_step = h / 6.0f;
+    p.goal_radius = c.goal_radius;
+    p.epsilon = c.epsilon;
+    p.ws_min = c.ws_min;
+    p.ws_max = c.ws_max;
+    volatile float range = c.ws_max - c.ws_min;
+    volatile float cell = range / (float)c.coarse_len;
+    volatile float cell2 = cell * cell;
+    p.ws_range = range;
+    p.cell_size = cell;
+    p.cell_volume = cell2 * cell;
+    p.coarse_len = c.coarse_len;
+    p.fine_len = c.fine_len;
+    p.regions = c.coarse_len * c.coarse_len * c.coarse_len;
+    p.fine_cells = c.fine_len * c.fine_len * c.fine_len;
+    p.v_min = c.v_min;
+    p.v_max = c.v_max;
+    for(int i = 0; i < 4; ++i)
+        {
+            p.u_min[i] = c.u_min[i];
+            volatile float span = c.u_max[i] - c.u_min[i];
+            p.u_span[i] = span;
+        }
+    p.nu = c.nu;
+    p.mu = c.mu;
+    p.gravity = c.gravity;
+    p.mass_inv = c.mass_inv;
+    if(c.model == KGMT_MODEL_QUADROTOR)
+        {
+            volatile float a = c.iy - c.iz, b = c.iz - c.ix, d = c.ix - c.iy;
+            p.iix = 1.0f / c.ix;
+            p.iiy = 1.0f / c.iy;
+            p.iiz = 1.0f / c.iz;
+            p.jx = a / c.ix;
+            p.jy = b / c.iy;
+            p.jz = d / c.iz;
+        }
+    p.seed = c.seed;
+    const uint32_t D = p.sample_dim;
+    if(goal)
+        for(int i = 0; i < 3; ++i) p.goal[i] = goal[i];
+    if(init)
+        for(uint32_t i = 0; i < D; ++i) p.init[i] = init[i];
+    p.n_obstacles = n_obstacles;
+    p.tiles_per_chain = L.tiles_per_chain;
+    p.tree = (float*)(chunk + L.tree);
+    p.parent = (int32_t*)(chunk + L.parent);
+    p.cost = (float*)(chunk + L.cost);
+    p.node_r1 = (int32_t*)(chunk + L.node_r1);
+    p.rep_old = (uint32_t*)(chunk + L.rep_old);
+    p.rep_new = (uint32_t*)(chunk + L.rep_new);
+    p.us = (float*)(chunk + L.us);
+    p.up = (int32_t*)(chunk + L.up);
+    p.ur1 = (int32_t*)(chunk + L.ur1);
+    p.uflag = (uint8_t*)(chunk + L.uflag);
+    p.counter = (int32_t*)(chunk + L.counter);
+    p.valid = (int32_t*)(chunk + L.valid);
+    p.score = (float*)(chunk + L.score);
+    p.marks = (uint64_t*)(chunk + L.marks);
+    p.newmarks = (uint64_t*)(chunk + L.newmarks);
+    p.tiles_old = (unsigned long long*)(chunk + L.tiles_old);
+    p.tiles_slot = (unsigned long long*)(chunk + L.tiles_slot);
+    p.path = (float*)(chunk + L.path);
+    p.obstacles = obstacles ? obstacles : (float4*)(chunk + L.obstacles);
+    return p;
+}
+
+kgmt_result to_result(const QueryState& s, uint64_t ticket)
+{
+    kgmt_result r;
+    std::memset(&r, 0, sizeof(r));
+    r.status = (int32_t)s.status;
+    r.iterations = s.itr;
+    r.tree_size = s.tree_size;
+    r.goal_index = s.status == KGMT_QUERY_SUCCESS ? s.goal_index : -1;
+    r.path_len = s.path_len;
+    r.samples_drawn = s.samples_drawn;
+    r.solve_ms = s.t_end > s.t_start ? (float)((double)(s.t_end - s.t_start) * 1e-6) : 0.0f;
+    r.ticket = ticket;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+__global__ void k_set_endpoints(QueryParams* P, uint32_t first, uint32_t count, const float* __restrict__ inits,
+                                const float* __restrict__ goals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= count) return;
+    QueryParams& p = P[first + i];
+    for(int j = 0; j < KGMT_MAX_SAMPLE_DIM; ++j) p.init[j] = inits[(size_t)i * KGMT_MAX_SAMPLE_DIM + j];
+    for(int j = 0; j < 3; ++j) p.goal[j] = goals[(size_t)i * KGMT_MAX_SAMPLE_DIM + j];
+}
+
+Engine::~Engine()
+{
+    if(graph_) cudaGraphExecDestroy(graph_);
+    for(auto& e : ev_)
+        if(e) cudaEventDestroy(e);
+    if(h_running_) cudaFreeHost(h_running_);
+    cudaFree(d_params_);
+    cudaFree(d_states_);
+    cudaFree(d_sched_);
+    cudaFree(d_tile_a_);
+    cudaFree(d_tile_c_);
+    cudaFree(d_tile_old_);
+    if(own_stream_ && stream_) cudaStreamDestroy(stream_);
+}
+
+LaunchArgs Engine::args() const { return LaunchArgs{d_params_, d_states_, d_sched_, d_tile_a_, d_tile_c_, d_tile_old_}; }
+
+kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_block, uint32_t iters_per_graph, bool use_graph)
+{
+    int dev_count = 0;
+    if(cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+        {
+            cudaGetLastError();
+            set_error("no CUDA device");
+            return KGMT_ERR_NO_DEVICE;
+        }
+    if(slots == 0)
+        {
+            set_error("engine needs at least one slot");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    slots_ = slots;
+    if(stream) stream_ = stream;
+    else
+        {
+            KGMT_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+            own_stream_ = true;
+        }
+    iters_per_graph_ = iters_per_graph ? iters_per_graph : 4;
+    use_graph_ = use_graph;
+    h_params_.assign(slots, QueryParams{});
+    KGMT_CUDA(cudaMalloc(&d_params_, sizeof(QueryParams) * slots), "cudaMalloc(params)");
+    KGMT_CUDA(cudaMalloc(&d_states_, sizeof(QueryState) * slots), "cudaMalloc(states)");
+    KGMT_CUDA(cudaMalloc(&d_sched_, sizeof(Sched)), "cudaMalloc(sched)");
+    KGMT_CUDA(cudaMalloc(&d_tile_a_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
+    KGMT_CUDA(cudaMalloc(&d_tile_c_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
+    KGMT_CUDA(cudaMalloc(&d_tile_old_, sizeof(uint32_t) * slots), "cudaMalloc(tiles)");
+    KGMT_CUDA(cudaMemsetAsync(d_states_, 0, sizeof(QueryState) * slots, stream_), "memset(states)");
+    KGMT_CUDA(cudaMemsetAsync(d_tile_a_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
+    KGMT_CUDA(cudaMemsetAsync(d_tile_c_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
+    KGMT_CUDA(cudaMemsetAsync(d_tile_old_, 0, sizeof(uint32_t) * slots, stream_), "memset");
+    KGMT_CUDA(cudaMallocHost(&h_running_, sizeof(uint32_t) * 2), "cudaMallocHost");
+    for(auto& e : ev_) KGMT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    return set_prop_block(prop_block ? prop_block : 256);
+}
+
+kgmt_status Engine::set_prop_block(uint32_t block)
+{
+    if(block != 64 && block != 128 && block != 256 && block != 512)
+        {
+            set_error("propagate block must be 64, 128, 256 or 512");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    prop_block_ = block;
+    int dev = 0, sms = 0;
+    KGMT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    KGMT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    grid_a_ = sms * propagate_blocks_per_sm((int)block);
+    grid_c_ = sms * append_blocks_per_sm();
+    Sched s;
+    std::memset(&s, 0, sizeof(s));
+    s.prop_tile = block;
+    KGMT_CUDA(cudaMemcpyAsync(d_sched_, &s, sizeof(s), cudaMemcpyHostToDevice, stream_), "upload(sched)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");
+    if(graph_)
+        {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+    return KGMT_OK;
+}
+
+kgmt_status Engine::upload_params(uint32_t first, uint32_t count)
+{
+    if(first + count > slots_)
+        {
+            set_error("upload_params: slot range out of bounds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    if(count == 0) return KGMT_OK;
+    // pageable source: the copy has completed when the call returns
+    KGMT_CUDA(cudaMemcpyAsync(d_params_ + first, h_params_.data() + first, sizeof(QueryParams) * count, cudaMemcpyHostToDevice, stream_),
+              "upload(params)");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::init_slots(uint32_t first, uint32_t count, const float* d_inits, const float* d_goals)
+{
+    if(first + count > slots_)
+        {
+            set_error("init_slots: slot range out of bounds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    if(count == 0) return KGMT_OK;
+    if(d_inits && d_goals)
+        {
+            k_set_endpoints<<<(count + 127) / 128, 128, 0, stream_>>>(d_params_, first, count, d_inits, d_goals);
+            KGMT_CUDA(cudaGetLastError(), "k_set_endpoints");
+        }
+    KGMT_CUDA(launch_admit(args(), first, count, stream_), "k_admit");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::set_active(uint32_t n_active)
+{
+    if(n_active > slots_)
+        {
+            set_error("set_active: more slots than the engine holds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    KGMT_CUDA(cudaMemcpyAsync(&d_sched_->n_slots, &n_active, sizeof(uint32_t), cudaMemcpyHostToDevice, stream_), "upload(n_slots)");
+    // n_active lives on the host stack: wait for the copy
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::schedule()
+{
+    KGMT_CUDA(launch_schedule(args(), stream_), "k_schedule");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::admit(uint32_t first, uint32_t count, uint32_t n_active, const float* d_inits, const float* d_goals)
+{
+    kgmt_status st = upload_params(first, count);
+    if(st == KGMT_OK) st = set_active(n_active);
+    if(st == KGMT_OK) st = init_slots(first, count, d_inits, d_goals);
+    if(st == KGMT_OK) st = schedule();
+    return st;
+}
+
+kgmt_status Engine::launch_iteration()
+{
+    const LaunchArgs a = args();
+    KGMT_CUDA(launch_propagate(a, (int)prop_block_, grid_a_, stream_), "k_propagate");
+    KGMT_CUDA(launch_score(a, (int)slots_, stream_), "k_score");
+    KGMT_CUDA(launch_append(a, grid_c_, stream_), "k_append");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::build_graph()
+{
+    cudaGraph_t g = nullptr;
+    KGMT_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    kgmt_status st = KGMT_OK;
+    for(uint32_t i = 0; i < iters_per_graph_ && st == KGMT_OK; ++i) st = launch_iteration();
+    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if(st != KGMT_OK)
+        {
+            if(g) cudaGraphDestroy(g);
+            return st;
+        }
+    KGMT_CUDA(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    return cuda_status(e, "cudaGraphInstantiate");
+}
+
+kgmt_status Engine::launch_unit()
+{
+    if(use_graph_)
+        {
+            if(!graph_)
+                {
+                    kgmt_status st = build_graph();
+                    if(st != KGMT_OK) return st;
+                }
+            KGMT_CUDA(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
+        }
+    else
+        {
+            for(uint32_t i = 0; i < iters_per_graph_; ++i)
+                {
+                    kgmt_status st = launch_iteration();
+                    if(st != KGMT_OK) return st;
+                }
+        }
+    iters_launched_ += iters_per_graph_;
+    return KGMT_OK;
+}
+
+kgmt_status Engine::run_until_done(uint32_t max_iters)
+{
+    const uint32_t G = iters_per_graph_;
+    const uint32_t max_units = (max_iters + G - 1) / G + 2;
+    for(uint32_t u = 0; u < max_units; ++u)
+        {
+            kgmt_status st = launch_unit();
+            if(st != KGMT_OK) return st;
+            KGMT_CUDA(cudaMemcpyAsync(&h_running_[u & 1], &d_sched_->running, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_),
+                      "poll(running)");
+            KGMT_CUDA(cudaEventRecord(ev_[u & 1], stream_), "cudaEventRecord");
+            if(u > 0)
+                {
+                    KGMT_CUDA(cudaEventSynchronize(ev_[(u - 1) & 1]), "cudaEventSynchronize");
+                    if(h_running_[(u - 1) & 1] == 0) break;
+                }
+        }
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::run_iterations(uint32_t iters)
+{
+    for(uint32_t i = 0; i < iters; ++i)
+        {
+            kgmt_status st = launch_iteration();
+            if(st != KGMT_OK) return st;
+        }
+    iters_launched_ += iters;
+    return KGMT_OK;
+}
+
+kgmt_status Engine::read_states(uint32_t first, uint32_t count, QueryState* out)
+{
+    if(count == 0) return KGMT_OK;
+    KGMT_CUDA(cudaMemcpyAsync(out, d_states_ + first, sizeof(QueryState) * count, cudaMemcpyDeviceToHost, stream_), "download(states)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::extract_paths(uint32_t n_active)
+{
+    KGMT_CUDA(launch_paths(args(), n_active, stream_), "k_paths");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::read_error(uint32_t* err)
+{
+    KGMT_CUDA(cudaMemcpyAsync(err, &d_sched_->error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "download(error)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return KGMT_OK;
+}
+
+}  // namespace kgmt

@@ -1,0 +1,116 @@
+// kgmt_engine.h -- host runtime of the planning engine.
+//
+// The engine owns the device-resident descriptors of up to `slots` queries
+// and replays the per-iteration kernel chain (optionally as a captured CUDA
+// graph) until every admitted query has finished.  The host only polls one
+// counter, one replay behind, so the GPU never waits on the CPU.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "kgmt_kernels.h"
+#include "kgmt_types.h"
+
+namespace kgmt {
+
+void set_error(const std::string& msg);
+kgmt_status cuda_status(cudaError_t e, const char* what);
+
+// first-fit allocator over one device allocation
+class DeviceArena {
+   public:
+    ~DeviceArena();
+    kgmt_status reserve(size_t bytes);  // (re)allocates when empty and too small
+    bool alloc(size_t bytes, size_t* offset);
+    void release(size_t offset);
+    void reset();
+    char* base() const { return base_; }
+    size_t capacity() const { return cap_; }
+    size_t in_use() const { return used_bytes_; }
+
+   private:
+    char* base_ = nullptr;
+    size_t cap_ = 0;
+    size_t used_bytes_ = 0;
+    std::map<size_t, size_t> free_;  // offset -> size
+    std::map<size_t, size_t> used_;
+};
+
+struct QueryLayout {
+    size_t tree, parent, cost, node_r1, rep_old, rep_new, us, up, ur1, uflag;
+    size_t counter, valid, score, marks, newmarks, tiles_old, tiles_slot, path, obstacles;
+    size_t total;
+    uint32_t tiles_per_chain;
+};
+
+kgmt_status validate_config(const kgmt_config& c);
+QueryLayout layout_of(const kgmt_config& c, uint32_t inline_obstacles);
+// derived constants in float exactly as the kernels expect them; buffers
+// point into `base + chunk_offset`; obstacles at `obstacles` (device)
+QueryParams make_params(const kgmt_config& c, const float* init, const float* goal, char* chunk, const QueryLayout& L, float4* obstacles,
+                        uint32_t n_obstacles);
+uint32_t sample_dim_of(int32_t model);
+kgmt_result to_result(const QueryState& s, uint64_t ticket);
+
+class Engine {
+   public:
+    ~Engine();
+    kgmt_status init(uint32_t slots, cudaStream_t stream, uint32_t prop_block, uint32_t iters_per_graph, bool use_graph);
+    uint32_t slots() const { return slots_; }
+    cudaStream_t stream() const { return stream_; }
+    QueryParams& host_params(uint32_t slot) { return h_params_[slot]; }
+    LaunchArgs args() const;
+
+    // uploads params of [first, first+count), initialises those slots and
+    // recomputes the schedule; n_active = slots the kernels look at.  With
+    // d_inits / d_goals (device rows of KGMT_MAX_SAMPLE_DIM floats) the start
+    // and goal are taken from device memory instead of the host params.
+    kgmt_status admit(uint32_t first, uint32_t count, uint32_t n_active, const float* d_inits = nullptr,
+                      const float* d_goals = nullptr);
+    // the pieces of admit, for callers that admit several slot ranges
+    kgmt_status upload_params(uint32_t first, uint32_t count);
+    kgmt_status init_slots(uint32_t first, uint32_t count, const float* d_inits = nullptr, const float* d_goals = nullptr);
+    kgmt_status set_active(uint32_t n_active);
+    kgmt_status schedule();
+    // runs iterations until no query is running (or max_iters + slack)
+    kgmt_status run_until_done(uint32_t max_iters);
+    // runs exactly `iters` iterations (served loop)
+    kgmt_status run_iterations(uint32_t iters);
+    kgmt_status read_states(uint32_t first, uint32_t count, QueryState* out);
+    kgmt_status extract_paths(uint32_t n_active);
+    kgmt_status read_error(uint32_t* err);
+    kgmt_status set_prop_block(uint32_t block);
+    uint32_t prop_block() const { return prop_block_; }
+    uint32_t iterations_launched() const { return iters_launched_; }
+
+   private:
+    kgmt_status launch_iteration();
+    kgmt_status launch_unit();
+    kgmt_status build_graph();
+
+    uint32_t slots_ = 0;
+    cudaStream_t stream_ = nullptr;
+    bool own_stream_ = false;
+    uint32_t prop_block_ = 256;
+    uint32_t iters_per_graph_ = 4;
+    bool use_graph_ = true;
+    int grid_a_ = 0, grid_c_ = 0;
+    QueryParams* d_params_ = nullptr;
+    QueryState* d_states_ = nullptr;
+    Sched* d_sched_ = nullptr;
+    uint32_t* d_tile_a_ = nullptr;
+    uint32_t* d_tile_c_ = nullptr;
+    uint32_t* d_tile_old_ = nullptr;
+    uint32_t* h_running_ = nullptr;  // pinned, 2 entries
+    cudaEvent_t ev_[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph_ = nullptr;
+    std::vector<QueryParams> h_params_;
+    uint32_t iters_launched_ = 0;
+};
+
+}  // namespace kgmt

@@ -1,0 +1,873 @@
+// kgmt_kernels.cu -- the per-iteration kernel chain of the KGMT planning loop.
+//
+// One iteration of every running query (reference: KGMT::plan loop body,
+// src/planners/KGMT.cu:84-95) is three launches with fixed shapes, so the
+// chain can be captured once in a CUDA graph and replayed:
+//
+//   k_propagate  KGMT::propagateFrontier + propagateFrontier_kernel1/2
+//                (KGMT.cu:167-299): one thread per sample, persistent blocks
+//                taking propagate tiles from a ticket counter, obstacles of
+//                the tile's query staged in shared memory by a bulk (TMA)
+//                copy, warp-aggregated atomics into the region histograms.
+//   k_score      Graph::updateVertices (Graph.cu:207-358): one block per
+//                query, region scores summed in a fixed order.
+//   k_append     KGMT::updateFrontier + updateFrontier_kernel
+//                (KGMT.cu:305-403) and the next iteration's frontier
+//                compaction / repeat expansion (KGMT.cu:167-181,
+//                Planner.cu:52-79): ordered stream compaction with
+//                decoupled look-back gives every accepted sample its tree
+//                index (an order-preserving "atomic append") and every
+//                re-activated node its frontier slot; the last tile of a
+//                query finalises it, the last query computes the schedule of
+//                the next iteration on the device.
+//
+// Frontier representation: instead of frontier flags over the whole tree and
+// two scans per iteration (KGMT.cu:170-181), the frontier of the next
+// iteration is built directly as two index lists -- re-activated old nodes
+// (repeat 1) followed by the nodes appended this iteration (repeat 15 or 1) --
+// which is the order the reference's scan over node indices produces.
+#include <cstdint>
+#include <climits>
+
+#include "kgmt_device.cuh"
+#include "kgmt_kernels.h"
+
+namespace kgmt {
+
+// ---------------------------------------------------------------------------
+// small device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+    return ok != 0;
+}
+
+// bulk global -> shared copy through the TMA engine; bytes % 16 == 0, both
+// addresses 16-byte aligned
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p)
+{
+    return *(const volatile unsigned long long*)p;
+}
+
+__device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned long long v)
+{
+    *(volatile unsigned long long*)p = v;
+}
+
+// last slot q with base[q] <= t (base is an exclusive prefix over n slots,
+// base[n] = total, t < total)
+__device__ __forceinline__ int find_slot(const uint32_t* __restrict__ base, int n, uint32_t t)
+{
+    int lo = 0, hi = n;
+    while(lo < hi)
+        {
+            int mid = (lo + hi + 1) >> 1;
+            if(base[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+    return lo;
+}
+
+// block-wide exclusive scan of one uint32 per thread; returns the exclusive
+// prefix, *total the block sum.  scratch: >= 33 words of shared memory.
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* scratch, uint32_t* total)
+{
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if(lane >= o) x += y;
+        }
+    if(lane == 31) scratch[warp] = x;
+    __syncthreads();
+    if(warp == 0)
+        {
+            uint32_t w = lane < NW ? scratch[lane] : 0u;
+            uint32_t z = w;
+#pragma unroll
+            for(int o = 1; o < 32; o <<= 1)
+                {
+                    uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+                    if(lane >= o) z += y;
+                }
+            if(lane < NW) scratch[lane] = z - w;
+            if(lane == NW - 1) scratch[32] = z;
+        }
+    __syncthreads();
+    uint32_t excl = scratch[warp] + x - v;
+    *total = scratch[32];
+    __syncthreads();
+    return excl;
+}
+
+// ---------------------------------------------------------------------------
+// decoupled look-back over one chain of tiles of one query.  Word layout:
+// bits 62-63 status (0 empty, 1 aggregate, 2 inclusive prefix), bits 0-61 the
+// value (the chains pack their counts so that sums never carry into the
+// status bits).  Tiles are taken in ticket order, so every predecessor is
+// held by a resident block; waits are bounded all the same.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kStAgg = 1ull << 62;
+constexpr unsigned long long kStIncl = 2ull << 62;
+constexpr unsigned long long kValMask = (1ull << 62) - 1;
+
+__device__ unsigned long long lookback(unsigned long long* tiles, int lt, uint32_t* error)
+{
+    unsigned long long prefix = 0;
+    for(int j = lt - 1; j >= 0; --j)
+        {
+            unsigned long long w = ld_volatile_u64(&tiles[j]);
+            uint32_t spins = 0;
+            while((w >> 62) == 0)
+                {
+                    if(++spins > kSpinLimit)
+                        {
+                            atomicOr(error, kErrLookbackTimeout);
+                            return prefix;
+                        }
+                    __nanosleep(32);
+                    w = ld_volatile_u64(&tiles[j]);
+                }
+            prefix += w & kValMask;
+            if((w >> 62) == 2) break;
+        }
+    return prefix;
+}
+
+// ---------------------------------------------------------------------------
+// schedule of the next iteration, computed by one block (the last query to
+// finalise, or the admission path): tiles per slot, prefix bases, running
+// count.  All threads of the calling block must enter.
+// ---------------------------------------------------------------------------
+__device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryState* __restrict__ S, Sched* sched, uint32_t* tile_a_base,
+                                 uint32_t* tile_c_base, uint32_t* tile_c_old)
+{
+    __shared__ uint32_t scratch[34];
+    __shared__ uint32_t carry[3];
+    const int n = (int)sched->n_slots;
+    const uint32_t prop_tile = sched->prop_tile;
+    if(threadIdx.x == 0) carry[0] = carry[1] = carry[2] = 0;
+    __syncthreads();
+    for(int base = 0; base < n; base += blockDim.x)
+        {
+            int q = base + threadIdx.x;
+            uint32_t ta = 0, tc = 0, told = 0, run = 0;
+            // other blocks finalised these states in this kernel: read past L1
+            if(q < n && __ldcg(&S[q].status) == KGMT_QUERY_RUNNING)
+                {
+                    uint32_t ns = __ldcg(&S[q].n_samples);
+                    ta = (ns + prop_tile - 1) / prop_tile;
+                    told = (__ldcg(&S[q].tree_size) + kTileC - 1) / kTileC;
+                    tc = told + (ns + kTileC - 1) / kTileC;
+                    run = 1;
+                }
+            uint32_t tot_a, tot_c, tot_r;
+            uint32_t ea = block_exclusive_scan<kAppendThreads>(ta, scratch, &tot_a);
+            uint32_t ec = block_exclusive_scan<kAppendThreads>(tc, scratch, &tot_c);
+            block_exclusive_scan<kAppendThreads>(run, scratch, &tot_r);
+            if(q < n)
+                {
+                    tile_a_base[q] = carry[0] + ea;
+                    tile_c_base[q] = carry[1] + ec;
+                    tile_c_old[q] = told;
+                }
+            __syncthreads();
+            if(threadIdx.x == 0)
+                {
+                    carry[0] += tot_a;
+                    carry[1] += tot_c;
+                    carry[2] += tot_r;
+                }
+            __syncthreads();
+        }
+    if(threadIdx.x == 0)
+        {
+            tile_a_base[n] = carry[0];
+            tile_c_base[n] = carry[1];
+            sched->tiles_a = carry[0];
+            sched->tiles_c = carry[1];
+            sched->running = carry[2];
+            sched->ticket_a = 0;
+            if(carry[2]) sched->iterations += 1;
+        }
+    __syncthreads();
+}
+
+// frontier entries R, samples per entry and samples of the next iteration
+// (KGMT.cu:183-201 with the capacity rule made safe)
+__device__ __forceinline__ void plan_samples(const QueryParams& P, QueryState& st)
+{
+    uint32_t R = st.n_react + st.w_new;
+    uint32_t free_slots = P.capacity - st.tree_size;
+    uint32_t spe = 0, ruse = R;
+    if(R > 0)
+        {
+            spe = free_slots / R;
+            if(spe > P.samples_per_node) spe = P.samples_per_node;
+            if(spe == 0)
+                {
+                    spe = 1;
+                    ruse = free_slots;
+                }
+        }
+    st.spe = spe;
+    st.n_samples = ruse * spe;
+}
+
+// ---------------------------------------------------------------------------
+// admission: root node, cleared region tables, first frontier (root x5)
+// ---------------------------------------------------------------------------
+__global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32_t first, uint32_t count)
+{
+    const uint32_t q = first + blockIdx.x;
+    if(blockIdx.x >= count) return;
+    const QueryParams& p = P[q];
+    for(uint32_t r = threadIdx.x; r < p.regions; r += blockDim.x)
+        {
+            p.counter[r] = 0;
+            p.valid[r] = 0;
+            p.score[r] = 0.0f;
+            p.marks[r] = 0ull;
+            p.newmarks[r] = 0ull;
+        }
+    for(uint32_t j = threadIdx.x; j < p.sample_dim; j += blockDim.x) p.tree[j] = p.init[j];
+    if(threadIdx.x < kRootRepeat) p.rep_new[threadIdx.x] = 0u;
+    if(threadIdx.x == 0)
+        {
+            p.parent[0] = -1;
+            p.cost[0] = 0.0f;
+            p.node_r1[0] = region_of(p, p.init[0], p.init[1], p.init[2]);
+            QueryState st = {};
+            st.status = KGMT_QUERY_RUNNING;
+            st.itr = 1;
+            st.tree_size = 1;
+            st.n_react = 0;
+            st.w_new = kRootRepeat;
+            st.goal_cand = INT_MAX;
+            st.goal_index = -1;
+            st.t_start = globaltimer();
+            plan_samples(p, st);
+            S[q] = st;
+        }
+}
+
+__global__ void k_schedule(const QueryParams* __restrict__ P, const QueryState* __restrict__ S, Sched* sched, uint32_t* tile_a_base,
+                           uint32_t* tile_c_base, uint32_t* tile_c_old)
+{
+    compute_schedule(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
+}
+
+// ---------------------------------------------------------------------------
+// propagate
+// ---------------------------------------------------------------------------
+struct PropCtx {
+    uint32_t itr, spe, n_react, n_samples;
+};
+
+template <int MODEL>
+__device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCtx& c, const float4* obs, uint32_t n_obs, uint32_t s,
+                                              bool live, QueryState* st)
+{
+    constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
+    constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
+    const unsigned full = 0xffffffffu;
+    int r1 = -1, r2 = 0;
+    bool ok = false, acc = false;
+    if(live)
+        {
+            const uint32_t e = s / c.spe;
+            const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
+            float x0[D], x1[D];
+            const float* src = p.tree + (size_t)par * D;
+#pragma unroll
+            for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
+            const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
+            const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
+            const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
+            const float u[8] = {u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), u01(b.y), u01(b.z), u01(b.w)};
+            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1);
+            else ok = propagate_di(p, x0, u, obs, n_obs, x1);
+            const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
+            r1 = cid.r1;
+            r2 = cid.r2;
+            float* dst = p.us + (size_t)s * D;
+#pragma unroll
+            for(int j = 0; j < D; ++j) dst[j] = x1[j];
+            p.up[s] = (int32_t)par;
+            p.ur1[s] = r1;
+            if(ok)
+                {
+                    const uint64_t bit = 1ull << r2;
+                    const bool fresh = (p.marks[r1] & bit) == 0ull;
+                    acc = (u[NC + 1] < p.score[r1]) || fresh;
+                    if((p.newmarks[r1] & bit) == 0ull) atomicOr((unsigned long long*)&p.newmarks[r1], (unsigned long long)bit);
+                }
+            p.uflag[s] = acc ? 1 : 0;
+        }
+    // warp-aggregated histogram updates (counter over all samples, valid over
+    // valid ones), then the per-query accepted count
+    const unsigned live_mask = __ballot_sync(full, live);
+    if(live)
+        {
+            const unsigned peers = __match_any_sync(live_mask, r1);
+            if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.counter[r1], __popc(peers));
+        }
+    const unsigned ok_mask = __ballot_sync(full, ok);
+    if(ok)
+        {
+            const unsigned peers = __match_any_sync(ok_mask, r1);
+            if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.valid[r1], __popc(peers));
+        }
+    const unsigned acc_mask = __ballot_sync(full, acc);
+    if((threadIdx.x & 31) == 0 && acc_mask) atomicAdd(&st->n_next, __popc(acc_mask));
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+                                                  const uint32_t* __restrict__ tile_base)
+{
+    extern __shared__ float4 s_obs[];  // kSmemObstacles * 2
+    __shared__ alignas(8) uint64_t bar;
+    __shared__ QueryParams s_p;
+    __shared__ PropCtx s_c;
+    __shared__ int s_tile;
+    __shared__ int s_q;
+    const uint32_t total = sched->tiles_a;
+    const int n_slots = (int)sched->n_slots;
+    if(blockIdx.x >= total) return;
+    if(threadIdx.x == 0)
+        {
+            mbar_init(&bar, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+    __syncthreads();
+    int cur_q = -1;
+    uint32_t phase = 0;
+    for(;;)
+        {
+            if(threadIdx.x == 0) s_tile = (int)atomicAdd(&sched->ticket_a, 1u);
+            __syncthreads();
+            const uint32_t t = (uint32_t)s_tile;
+            if(t >= total) break;
+            if(threadIdx.x == 0) s_q = find_slot(tile_base, n_slots, t);
+            __syncthreads();
+            const int q = s_q;
+            if(q != cur_q)
+                {
+                    // stage the query's parameters and obstacles
+                    const uint32_t* src = (const uint32_t*)&P[q];
+                    uint32_t* dst = (uint32_t*)&s_p;
+                    for(int i = threadIdx.x; i < (int)(sizeof(QueryParams) / 4); i += NT) dst[i] = src[i];
+                    if(threadIdx.x == 0)
+                        {
+                            const QueryState& st = S[q];
+                            s_c.itr = st.itr;
+                            s_c.spe = st.spe;
+                            s_c.n_react = st.n_react;
+                            s_c.n_samples = st.n_samples;
+                            const uint32_t n_obs = P[q].n_obstacles;
+                            if(n_obs > 0 && n_obs <= (uint32_t)kSmemObstacles)
+                                {
+                                    fence_proxy_async_smem();
+                                    const uint32_t bytes = n_obs * 32u;
+                                    mbar_expect_tx(&bar, bytes);
+                                    bulk_copy_g2s(s_obs, P[q].obstacles, bytes, &bar);
+                                }
+                        }
+                    __syncthreads();
+                    if(s_p.n_obstacles > 0 && s_p.n_obstacles <= (uint32_t)kSmemObstacles)
+                        {
+                            uint32_t spins = 0;
+                            while(!mbar_try_wait(&bar, phase))
+                                if(++spins > kSpinLimit)
+                                    {
+                                        if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
+                                        break;
+                                    }
+                            phase ^= 1u;
+                        }
+                    cur_q = q;
+                }
+            const uint32_t lt = t - tile_base[q];
+            const uint32_t s = lt * NT + threadIdx.x;
+            const bool live = s < s_c.n_samples;
+            const float4* obs = s_p.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : s_p.obstacles;
+            if(s_p.model == KGMT_MODEL_QUADROTOR) propagate_one<KGMT_MODEL_QUADROTOR>(s_p, s_c, obs, s_p.n_obstacles, s, live, &S[q]);
+            else propagate_one<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, obs, s_p.n_obstacles, s, live, &S[q]);
+            __syncthreads();
+        }
+}
+
+// ---------------------------------------------------------------------------
+// score: Graph::updateVertices with all regions scored and a fixed summation
+// order (lane l of kScoreLanes sums regions l, l+256, ... then a halving tree)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kScoreLanes) k_score(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+                                                       const uint32_t* __restrict__ tile_c_base,
+                                                       const uint32_t* __restrict__ tile_c_old)
+{
+    __shared__ float lanes[kScoreLanes];
+    const int q = blockIdx.x;
+    if(q == 0 && threadIdx.x == 0)
+        {
+            sched->ticket_c = 0;
+            sched->finalized = 0;
+        }
+    if(q >= (int)sched->n_slots) return;
+    QueryState& st = S[q];
+    if(st.status != KGMT_QUERY_RUNNING) return;
+    const QueryParams& p = P[q];
+    const float F = (float)p.fine_cells;
+    float acc = 0.0f;
+    for(uint32_t r = threadIdx.x; r < p.regions; r += kScoreLanes)
+        {
+            const uint64_t m = p.marks[r] | p.newmarks[r];
+            p.marks[r] = m;
+            p.newmarks[r] = 0ull;
+            const int32_t nv = p.valid[r];
+            float raw = 0.0f;
+            if(nv > 0)
+                {
+                    const int32_t n = p.counter[r];
+                    const float cov = (float)__popcll(m) / F;
+                    const float a = p.epsilon + (float)nv;
+                    const float b = a + (float)(n - nv);
+                    const float fv = (a / b) * p.cell_volume;
+                    const float f2 = fv * fv;
+                    const float f4 = f2 * f2;
+                    const float nf = (float)n;
+                    const float den = (1.0f + cov) * (1.0f + nf * nf);
+                    raw = f4 / den;
+                }
+            p.score[r] = raw;
+            acc = acc + raw;
+        }
+    lanes[threadIdx.x] = acc;
+    __syncthreads();
+#pragma unroll
+    for(int stride = kScoreLanes / 2; stride >= 1; stride >>= 1)
+        {
+            if((int)threadIdx.x < stride) lanes[threadIdx.x] = lanes[threadIdx.x] + lanes[threadIdx.x + stride];
+            __syncthreads();
+        }
+    const float total = lanes[0];
+    for(uint32_t r = threadIdx.x; r < p.regions; r += kScoreLanes)
+        {
+            if(p.valid[r] == 0) p.score[r] = 1.0f;
+            else p.score[r] = total > 0.0f ? p.epsilon + p.score[r] / total : p.epsilon;
+        }
+    // clear this iteration's look-back words and per-iteration accumulators
+    const uint32_t n_old = tile_c_old[q];
+    const uint32_t n_slot = (tile_c_base[q + 1] - tile_c_base[q]) - n_old;
+    for(uint32_t i = threadIdx.x; i < n_old; i += kScoreLanes) p.tiles_old[i] = 0ull;
+    for(uint32_t i = threadIdx.x; i < n_slot; i += kScoreLanes) p.tiles_slot[i] = 0ull;
+    if(threadIdx.x == 0)
+        {
+            st.score_total = total;
+            // KGMT.cu:387-388
+            const float ta = 1.0f - (float)(st.tree_size + st.n_next) / (float)p.capacity;
+            const float ie = (float)st.itr * p.epsilon;
+            const double t = (double)ta;
+            const double t5 = ((t * t) * (t * t)) * t;
+            st.f_accept = (float)((double)ie * t5);
+            st.tiles_done = 0;
+            st.react_total = 0;
+            st.acc_total = 0;
+            st.w_total = 0;
+            st.goal_cand = INT_MAX;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// append / re-activation / frontier build
+// ---------------------------------------------------------------------------
+__device__ void finalize_query(const QueryParams& p, QueryState& st, Sched* sched)
+{
+    // runs on one thread; the per-iteration totals were accumulated by other
+    // blocks' atomics, so they are read past L1
+    const uint32_t acc_total = __ldcg(&st.acc_total);
+    const int32_t goal_cand = __ldcg(&st.goal_cand);
+    if(acc_total != __ldcg(&st.n_next)) atomicOr(&sched->error, kErrAppendMismatch);
+    st.tree_size += acc_total;
+    st.samples_drawn += st.n_samples;
+    if(goal_cand != INT_MAX)
+        {
+            st.status = KGMT_QUERY_SUCCESS;
+            st.goal_index = goal_cand;
+        }
+    else if(st.itr >= p.max_iterations) st.status = KGMT_QUERY_ITER_LIMIT;
+    else if(st.tree_size >= p.capacity) st.status = KGMT_QUERY_CAPACITY;
+    if(st.status != KGMT_QUERY_RUNNING)
+        {
+            st.t_end = globaltimer();
+            return;
+        }
+    st.n_react = __ldcg(&st.react_total);
+    st.w_new = __ldcg(&st.w_total);
+    st.itr += 1;
+    st.n_next = 0;
+    plan_samples(p, st);
+}
+
+__global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+                                                           uint32_t* tile_a_base, uint32_t* tile_c_base, uint32_t* tile_c_old)
+{
+    __shared__ uint32_t scratch[34];
+    __shared__ int s_tile, s_q, s_glob;
+    __shared__ unsigned long long s_prefix;
+    const uint32_t total = sched->tiles_c;
+    const int n_slots = (int)sched->n_slots;
+    if(blockIdx.x >= total) return;
+    for(;;)
+        {
+            if(threadIdx.x == 0)
+                {
+                    const uint32_t t = atomicAdd(&sched->ticket_c, 1u);
+                    s_tile = (int)t;
+                    s_q = t < total ? find_slot(tile_c_base, n_slots, t) : -1;
+                    s_glob = 0;
+                }
+            __syncthreads();
+            const uint32_t t = (uint32_t)s_tile;
+            if(t >= total) break;
+            const int q = s_q;
+            const QueryParams& p = P[q];
+            QueryState& st = S[q];
+            const uint32_t lt = t - tile_c_base[q];
+            const uint32_t n_old = tile_c_old[q];
+            const uint32_t itr = st.itr;
+            const uint32_t tree_size = st.tree_size;
+            if(lt < n_old)
+                {
+                    // ---- re-activation of old nodes (KGMT.cu:364-377) ----
+                    const uint32_t i0 = lt * kTileC + threadIdx.x * 4;
+                    const float fa = st.f_accept;
+                    const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
+                    uint32_t flags = 0, cnt = 0;
+#pragma unroll
+                    for(int j = 0; j < 4; ++j)
+                        {
+                            const uint32_t i = i0 + j;
+                            if(i < tree_size)
+                                {
+                                    const U4 r = philox4x32_10(i, itr, 1u, 0u, k0, k1);
+                                    const float ur = u01(r.x);
+                                    if(ur <= p.score[p.node_r1[i]] + fa)
+                                        {
+                                            flags |= 1u << j;
+                                            ++cnt;
+                                        }
+                                }
+                        }
+                    uint32_t agg;
+                    const uint32_t excl = block_exclusive_scan<kAppendThreads>(cnt, scratch, &agg);
+                    if(threadIdx.x == 0)
+                        {
+                            unsigned long long prefix = 0;
+                            if(lt == 0) st_volatile_u64(&p.tiles_old[0], kStIncl | agg);
+                            else
+                                {
+                                    st_volatile_u64(&p.tiles_old[lt], kStAgg | agg);
+                                    prefix = lookback(p.tiles_old, (int)lt, &sched->error);
+                                    __threadfence();
+                                    st_volatile_u64(&p.tiles_old[lt], kStIncl | (prefix + agg));
+                                }
+                            s_prefix = prefix;
+                            atomicAdd(&st.react_total, agg);
+                        }
+                    __syncthreads();
+                    uint32_t pos = (uint32_t)s_prefix + excl;
+#pragma unroll
+                    for(int j = 0; j < 4; ++j)
+                        if(flags & (1u << j)) p.rep_old[pos++] = i0 + j;
+                }
+            else
+                {
+                    // ---- ordered append of accepted samples (KGMT.cu:317-362) ----
+                    const uint32_t lts = lt - n_old;
+                    const uint32_t s0 = lts * kTileC + threadIdx.x * 4;
+                    const uint32_t ns = st.n_samples;
+                    uint32_t acc_bits = 0, ca = 0, cw = 0;
+                    uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+                    for(int j = 0; j < 4; ++j)
+                        {
+                            const uint32_t s = s0 + j;
+                            if(s < ns && p.uflag[s])
+                                {
+                                    acc_bits |= 1u << j;
+                                    ++ca;
+                                    w[j] = p.valid[p.ur1[s]] < kSparseValidLimit ? kRepeatSparse : kRepeatDense;
+                                    cw += w[j];
+                                }
+                        }
+                    uint32_t agg;
+                    const uint32_t excl = block_exclusive_scan<kAppendThreads>((ca << 16) | cw, scratch, &agg);
+                    const uint32_t agg_a = agg >> 16, agg_w = agg & 0xffffu;
+                    if(threadIdx.x == 0)
+                        {
+                            const unsigned long long val = ((unsigned long long)agg_a << 32) | agg_w;
+                            unsigned long long prefix = 0;
+                            if(lts == 0) st_volatile_u64(&p.tiles_slot[0], kStIncl | val);
+                            else
+                                {
+                                    st_volatile_u64(&p.tiles_slot[lts], kStAgg | val);
+                                    prefix = lookback(p.tiles_slot, (int)lts, &sched->error);
+                                    __threadfence();
+                                    st_volatile_u64(&p.tiles_slot[lts], kStIncl | (prefix + val));
+                                }
+                            s_prefix = prefix;
+                            atomicAdd(&st.acc_total, agg_a);
+                            atomicAdd(&st.w_total, agg_w);
+                        }
+                    __syncthreads();
+                    const unsigned long long pre = s_prefix;
+                    uint32_t ia = tree_size + (uint32_t)(pre >> 32) + (excl >> 16);
+                    uint32_t iw = (uint32_t)(pre & 0xffffffffull) + (excl & 0xffffu);
+                    const int D = (int)p.sample_dim;
+#pragma unroll
+                    for(int j = 0; j < 4; ++j)
+                        {
+                            if(!(acc_bits & (1u << j))) continue;
+                            const uint32_t s = s0 + j;
+                            const uint32_t idx = ia++;
+                            const float* src = p.us + (size_t)s * D;
+                            float* dst = p.tree + (size_t)idx * D;
+                            for(int c = 0; c < D; ++c) dst[c] = src[c];
+                            p.parent[idx] = p.up[s];
+                            const float dist = goal_distance(src[0], src[1], src[2], p);
+                            p.cost[idx] = dist;
+                            p.node_r1[idx] = p.ur1[s];
+                            for(uint32_t r = 0; r < w[j]; ++r, ++iw)
+                                if(iw < p.capacity) p.rep_new[iw] = idx;
+                            if(dist < p.goal_radius) atomicMin(&st.goal_cand, (int)idx);
+                        }
+                }
+            // ---- tile done; the last tile of the query finalises it ----
+            __syncthreads();
+            if(threadIdx.x == 0)
+                {
+                    __threadfence();
+                    const uint32_t n_tiles = tile_c_base[q + 1] - tile_c_base[q];
+                    const uint32_t done = atomicAdd(&st.tiles_done, 1u);
+                    if(done == n_tiles - 1)
+                        {
+                            __threadfence();
+                            finalize_query(p, st, sched);
+                            __threadfence();
+                            const uint32_t f = atomicAdd(&sched->finalized, 1u);
+                            if(f == sched->running - 1) s_glob = 1;
+                        }
+                }
+            __syncthreads();
+            if(s_glob)
+                {
+                    __threadfence();
+                    compute_schedule(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
+                }
+            __syncthreads();
+        }
+}
+
+// ---------------------------------------------------------------------------
+// goal -> root path walk for finished queries (KGMT.cu:344-360)
+// ---------------------------------------------------------------------------
+__global__ void k_paths(const QueryParams* __restrict__ P, QueryState* S, uint32_t n)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if(q >= n) return;
+    QueryState& st = S[q];
+    if(st.status != KGMT_QUERY_SUCCESS || st.path_len != 0) return;
+    const QueryParams& p = P[q];
+    const uint32_t D = p.sample_dim;
+    const uint32_t max_rows = p.max_iterations + 2;
+    int32_t i = st.goal_index;
+    uint32_t len = 0;
+    while(i >= 0 && len < max_rows)
+        {
+            const float* src = p.tree + (size_t)i * D;
+            float* dst = p.path + (size_t)len * D;
+            for(uint32_t c = 0; c < D; ++c) dst[c] = src[c];
+            ++len;
+            i = p.parent[i];
+        }
+    st.path_len = len;
+}
+
+// ---------------------------------------------------------------------------
+// obstacles: [n][6] rows (min xyz, max xyz) -> [n][2] float4 in the arena
+// ---------------------------------------------------------------------------
+__global__ void k_stage_obstacles(const float* __restrict__ src, float4* dst, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const float* r = src + (size_t)i * 6;
+    dst[2 * i] = make_float4(r[0], r[1], r[2], 0.0f);
+    dst[2 * i + 1] = make_float4(r[3], r[4], r[5], 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// function-level propagation with explicit uniforms
+// ---------------------------------------------------------------------------
+__global__ void k_propagate_samples(const QueryParams p, const float* __restrict__ x0, const float* __restrict__ uni,
+                                    const float* __restrict__ obs_rows, uint32_t n_obs, uint32_t n, float* x1, uint8_t* valid,
+                                    int32_t* r1, int32_t* r2)
+{
+    extern __shared__ float4 s_obs[];
+    for(uint32_t i = threadIdx.x; i < n_obs; i += blockDim.x)
+        {
+            const float* r = obs_rows + (size_t)i * 6;
+            s_obs[2 * i] = make_float4(r[0], r[1], r[2], 0.0f);
+            s_obs[2 * i + 1] = make_float4(r[3], r[4], r[5], 0.0f);
+        }
+    __syncthreads();
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if(s >= n) return;
+    const int D = (int)p.sample_dim;
+    float a[kMaxSampleDim], b[kMaxSampleDim], u[8];
+    for(int j = 0; j < D; ++j) a[j] = x0[(size_t)s * D + j];
+    for(int j = 0; j < 8; ++j) u[j] = uni[(size_t)s * 8 + j];
+    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b) : propagate_di(p, a, u, s_obs, n_obs, b);
+    for(int j = 0; j < D; ++j) x1[(size_t)s * D + j] = b[j];
+    valid[s] = ok ? 1 : 0;
+    const CellIds c = cell_ids(p, b[0], b[1], b[2]);
+    if(r1) r1[s] = c.r1;
+    if(r2) r2[s] = c.r2;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launch wrappers
+// ---------------------------------------------------------------------------
+template <int NT>
+static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, cudaStream_t s)
+{
+    k_propagate<NT><<<grid, NT, kSmemObstacles * 2 * sizeof(float4), s>>>(a.params, a.states, a.sched, a.tile_a_base);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_propagate(const LaunchArgs& a, int block, int grid, cudaStream_t s)
+{
+    switch(block)
+        {
+            case 64: return launch_propagate_t<64>(a, grid, s);
+            case 128: return launch_propagate_t<128>(a, grid, s);
+            case 512: return launch_propagate_t<512>(a, grid, s);
+            default: return launch_propagate_t<256>(a, grid, s);
+        }
+}
+
+int propagate_blocks_per_sm(int block)
+{
+    int n = 0;
+    const size_t smem = kSmemObstacles * 2 * sizeof(float4);
+    switch(block)
+        {
+            case 64: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<64>, 64, smem); break;
+            case 128: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<128>, 128, smem); break;
+            case 512: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<512>, 512, smem); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<256>, 256, smem); break;
+        }
+    return n > 0 ? n : 1;
+}
+
+int append_blocks_per_sm()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_append, kAppendThreads, 0);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_score(const LaunchArgs& a, int n_slots, cudaStream_t s)
+{
+    k_score<<<n_slots, kScoreLanes, 0, s>>>(a.params, a.states, a.sched, a.tile_c_base, a.tile_c_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s)
+{
+    k_append<<<grid, kAppendThreads, 0, s>>>(a.params, a.states, a.sched, a.tile_a_base, a.tile_c_base, a.tile_c_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s)
+{
+    if(count == 0) return cudaSuccess;
+    k_admit<<<count, 256, 0, s>>>(a.params, a.states, first, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schedule(const LaunchArgs& a, cudaStream_t s)
+{
+    k_schedule<<<1, kAppendThreads, 0, s>>>(a.params, a.states, a.sched, a.tile_a_base, a.tile_c_base, a.tile_c_old);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s)
+{
+    if(n == 0) return cudaSuccess;
+    k_paths<<<(n + 127) / 128, 128, 0, s>>>(a.params, a.states, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, cudaStream_t s)
+{
+    if(n == 0) return cudaSuccess;
+    k_stage_obstacles<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, const float* u, const float* obs, uint32_t n_obs, uint32_t n,
+                                     float* x1, uint8_t* valid, int32_t* r1, int32_t* r2, cudaStream_t s)
+{
+    if(n == 0) return cudaSuccess;
+    const size_t smem = (size_t)n_obs * 2 * sizeof(float4);
+    if(smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(k_propagate_samples, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if(e != cudaSuccess) return e;
+        }
+    k_propagate_samples<<<(n + 127) / 128, 128, smem, s>>>(p, x0, u, obs, n_obs, n, x1, valid, r1, r2);
+    return cudaGetLastError();
+}
+
+}  // namespace kgmt

@@ -1,0 +1,30 @@
+// kgmt_kernels.h -- host-side launch wrappers of the kernel chain.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kgmt_types.h"
+
+namespace kgmt {
+
+struct LaunchArgs {
+    const QueryParams* params;
+    QueryState* states;
+    Sched* sched;
+    uint32_t* tile_a_base;  // [slots + 1]
+    uint32_t* tile_c_base;  // [slots + 1]
+    uint32_t* tile_c_old;   // [slots]
+};
+
+cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s);
+cudaError_t launch_schedule(const LaunchArgs& a, cudaStream_t s);
+cudaError_t launch_propagate(const LaunchArgs& a, int block, int grid, cudaStream_t s);
+cudaError_t launch_score(const LaunchArgs& a, int n_slots, cudaStream_t s);
+cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s);
+cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, cudaStream_t s);
+cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, const float* u, const float* obs, uint32_t n_obs, uint32_t n,
+                                     float* x1, uint8_t* valid, int32_t* r1, int32_t* r2, cudaStream_t s);
+int propagate_blocks_per_sm(int block);
+int append_blocks_per_sm();
+
+}  // namespace kgmt

@@ -1,0 +1,113 @@
+// kgmt_types.h -- device-resident descriptors of the planning engine.
+//
+// One engine runs any number of independent queries ("slots").  Per slot:
+//   QueryParams  immutable after admission: config values pre-derived in
+//                float, and the device pointers of the slot's buffers
+//   QueryState   mutable loop state (iteration, tree size, frontier sizes)
+// and one Sched per engine: the device-computed schedule of the next
+// iteration (tiles per slot, tickets), so the host never reads sizes back.
+#pragma once
+#include <cstdint>
+
+#include "../../include/kgmt.h"
+
+namespace kgmt {
+
+constexpr int kMaxSampleDim = KGMT_MAX_SAMPLE_DIM;
+constexpr int kScoreLanes = 256;        // fixed summation shape of the score total
+constexpr int kTileC = 1024;            // elements per append / re-activation tile
+constexpr int kAppendThreads = 256;     // threads per append block (4 elements each)
+constexpr int kRootRepeat = 5;          // KGMT.cu:67
+constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
+constexpr int kRepeatDense = 1;         // KGMT.cu:338-339
+constexpr int kSparseValidLimit = 10;   // KGMT.cu:336
+constexpr int kSmemObstacles = 1024;    // boxes staged in shared memory per block
+constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a device-side wait gives up
+
+// error bits in Sched::error
+constexpr uint32_t kErrLookbackTimeout = 1u;
+constexpr uint32_t kErrCopyTimeout = 2u;
+constexpr uint32_t kErrAppendMismatch = 4u;
+
+struct QueryParams {
+    int32_t model;
+    int32_t di_rule;
+    uint32_t capacity;
+    uint32_t samples_per_node;
+    uint32_t max_iterations;
+    uint32_t min_steps, max_steps;
+    uint32_t sample_dim;
+    float step_span;  // (float)(max_steps - min_steps + 1)
+    float step_size, half_step, sixth_step;
+    float goal_radius, epsilon;
+    float ws_min, ws_max, ws_range, cell_size, cell_volume;
+    uint32_t coarse_len, fine_len, regions, fine_cells;
+    float v_min, v_max;
+    float u_min[4], u_span[4];
+    float nu, mu, gravity, mass_inv;
+    float iix, iiy, iiz;  // 1 / I
+    float jx, jy, jz;     // (Iy - Iz) / Ix, (Iz - Ix) / Iy, (Ix - Iy) / Iz
+    uint64_t seed;
+    float goal[3];
+    float init[kMaxSampleDim];
+    uint32_t n_obstacles;
+    uint32_t tiles_per_chain;  // capacity of each tile-state chain
+    // buffers (device pointers into the engine arena)
+    float* tree;          // [capacity][sample_dim]   d_treeSamples_
+    int32_t* parent;      // [capacity]               d_treeSamplesParentIdxs_
+    float* cost;          // [capacity]               d_treeSampleCosts_
+    int32_t* node_r1;     // [capacity] coarse region of each node
+    uint32_t* rep_old;    // [capacity] re-activated nodes (repeat 1 each)
+    uint32_t* rep_new;    // [capacity] new nodes, each repeated 15 or 1 times
+    float* us;            // [capacity][sample_dim] unexplored samples
+    int32_t* up;          // [capacity] parent of each sample
+    int32_t* ur1;         // [capacity] region of each sample
+    uint8_t* uflag;       // [capacity] sample joins the tree
+    int32_t* counter;     // [regions] samples per region          (d_counterArray_)
+    int32_t* valid;       // [regions] valid samples per region    (d_validCounterArray_)
+    float* score;         // [regions]                              (d_vertexScoreArray_)
+    uint64_t* marks;      // [regions] fine cells visited, one bit per cell (d_activeSubVertices_)
+    uint64_t* newmarks;   // [regions] cells first visited this iteration
+    float4* obstacles;    // [n_obstacles][2] (min.xyz, -), (max.xyz, -)
+    unsigned long long* tiles_old;   // [tiles_per_chain] look-back words, re-activation chain
+    unsigned long long* tiles_slot;  // [tiles_per_chain] look-back words, append chain
+    float* path;          // [max_iterations + 2][sample_dim] goal -> root rows
+};
+
+struct QueryState {
+    uint32_t status;      // KGMT_QUERY_*
+    uint32_t itr;         // iteration being run (1-based), h_itr_
+    uint32_t tree_size;   // h_treeSize_
+    uint32_t n_react;     // rep_old length
+    uint32_t w_new;       // rep_new length (sum of repeats)
+    uint32_t spe;         // samples per frontier entry this iteration
+    uint32_t n_samples;   // samples this iteration
+    uint32_t n_next;      // accepted samples (atomic, propagate)
+    int32_t goal_cand;    // smallest new tree index in the goal ball (atomicMin)
+    int32_t goal_index;
+    uint32_t tiles_done;  // append/re-activation tiles finished this iteration
+    uint32_t react_total; // atomics of the append kernel
+    uint32_t acc_total;
+    uint32_t w_total;
+    float f_accept;
+    float score_total;
+    uint32_t samples_drawn;
+    uint32_t path_len;
+    unsigned long long t_start;  // %globaltimer_lo at admission (ns)
+    unsigned long long t_end;
+};
+
+struct Sched {
+    uint32_t n_slots;
+    uint32_t running;
+    uint32_t tiles_a;     // propagate tiles this iteration
+    uint32_t tiles_c;     // append / re-activation tiles this iteration
+    uint32_t ticket_a;
+    uint32_t ticket_c;
+    uint32_t finalized;
+    uint32_t error;
+    uint32_t iterations;  // engine iterations launched with work
+    uint32_t prop_tile;   // samples per propagate tile (= propagate block size)
+};
+
+}  // namespace kgmt

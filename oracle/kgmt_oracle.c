@@ -242,6 +242,19 @@ static int motion_valid_d(const double* p0, const double* p1, const float* obs, 
     return 1;
 }
 
+/* distance of a state to the velocity and workspace thresholds */
+static double bound_margin_d(const ko_config* c, const double* pos, const double* vel)
+{
+    double m = 1e30;
+    for(int d = 0; d < 3; ++d)
+        {
+            double t[4] = {fabs(vel[d] - c->v_min), fabs(vel[d] - c->v_max), fabs(pos[d] - c->ws_min), fabs(pos[d] - c->ws_max)};
+            for(int i = 0; i < 4; ++i)
+                if(t[i] < m) m = t[i];
+        }
+    return m;
+}
+
 static double face_margin_d(const double* p0, const double* p1, const float* obs, uint32_t n_obs)
 {
     double bmin[3], bmax[3], m = 1e30;
@@ -250,16 +263,21 @@ static double face_margin_d(const double* p0, const double* p1, const float* obs
             if(p0[d] > p1[d]) bmin[d] = p1[d], bmax[d] = p0[d];
             else bmin[d] = p0[d], bmax[d] = p1[d];
         }
+    /* signed separation of the step box from a box: max over axes of
+     * max(obsMin - bbMax, bbMin - obsMax); the verdict for that box flips
+     * only when it crosses zero */
     for(uint32_t o = 0; o < n_obs; ++o)
         {
             const float* b = obs + 6 * (size_t)o;
+            double sep = -1e30;
             for(int d = 0; d < 3; ++d)
                 {
-                    double a1 = fabs(bmax[d] - (double)b[d]);
-                    double a2 = fabs((double)b[3 + d] - bmin[d]);
-                    if(a1 < m) m = a1;
-                    if(a2 < m) m = a2;
+                    double a1 = (double)b[d] - bmax[d];
+                    double a2 = bmin[d] - (double)b[3 + d];
+                    double s = a1 > a2 ? a1 : a2;
+                    if(s > sep) sep = s;
                 }
+            if(fabs(sep) < m) m = fabs(sep);
         }
     return m;
 }
@@ -351,6 +369,8 @@ static int prop_di_d(const ko_config* c, const float* x0, const float* u, const 
                     p[d] = p[d] + (sum * h) / 6.0;
                 }
             for(int d = 0; d < 3; ++d) v[d] = v[d] + a[d] * h;
+            double bm = bound_margin_d(c, p, v);
+            if(bm < m) m = bm;
             if(v[0] < c->v_min || v[0] > c->v_max || v[1] < c->v_min || v[1] > c->v_max || v[2] < c->v_min || v[2] > c->v_max)
                 {
                     ok = 0;
@@ -503,6 +523,8 @@ static int prop_quad_d(const ko_config* c, const float* x0, const float* u, cons
             for(int j = 0; j < 12; ++j) t[j] = s[j] + h * k3[j];
             quad_ode_d(c, t, ctrl, k4);
             for(int j = 0; j < 12; ++j) s[j] += h / 6.0 * (k1[j] + 2.0 * k2[j] + 2.0 * k3[j] + k4[j]);
+            double bm = bound_margin_d(c, s, s + 6);
+            if(bm < m) m = bm;
             if(s[6] < c->v_min || s[6] > c->v_max || s[7] < c->v_min || s[7] > c->v_max || s[8] < c->v_min || s[8] > c->v_max)
                 {
                     ok = 0;
@@ -562,7 +584,7 @@ void ko_propagate_f64(const ko_config* c, const float* x0, const float* u, const
         }
 }
 
-double ko_face_margin_f64(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs)
+double ko_verdict_margin_f64(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs)
 {
     double y[KO_MAX_SAMPLE_DIM], m = 1e30;
     if(c->model == KO_MODEL_QUADROTOR) prop_quad_d(c, x0, u, obstacles, n_obs, y, &m);

@@ -121,7 +121,7 @@ void ko_propagate_f64(const ko_config* c, const float* x0, const float* u, const
                       double* x1, uint8_t* valid);
 /* minimum distance (over steps taken in FP64) between the swept step boxes
  * and any obstacle face; used to classify verdict mismatches */
-double ko_face_margin_f64(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs);
+double ko_verdict_margin_f64(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs);
 
 /* Region score update (Graph.cu:311-358 with the defects fixed) */
 void ko_score_update(const ko_config* c, const int32_t* counter, const int32_t* valid, uint64_t* marks, uint64_t* newmarks,

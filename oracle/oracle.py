@@ -85,8 +85,8 @@ def load():
         lib.ko_distance.argtypes = [fp, fp]
         lib.ko_propagate_f32.argtypes = [cfgp, fp, fp, fp, C.c_uint32, C.c_uint32, fp, u8p, i32p, i32p]
         lib.ko_propagate_f64.argtypes = [cfgp, fp, fp, fp, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), u8p]
-        lib.ko_face_margin_f64.restype = C.c_double
-        lib.ko_face_margin_f64.argtypes = [cfgp, fp, fp, fp, C.c_uint32]
+        lib.ko_verdict_margin_f64.restype = C.c_double
+        lib.ko_verdict_margin_f64.argtypes = [cfgp, fp, fp, fp, C.c_uint32]
         lib.ko_score_update.argtypes = [cfgp, i32p, i32p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), fp, fp]
         lib.ko_f_accept.restype = f
         lib.ko_f_accept.argtypes = [C.c_uint32, f, C.c_uint32, C.c_uint32, C.c_uint32]
@@ -175,10 +175,10 @@ def propagate_f64(cfg, x0, u, obstacles):
     return x1, valid
 
 
-def face_margin_f64(cfg, x0, u, obstacles) -> float:
+def verdict_margin_f64(cfg, x0, u, obstacles) -> float:
     k = to_ko(cfg)
     obs = _f32(obstacles).reshape(-1, 6)
-    return float(load().ko_face_margin_f64(C.byref(k), _ptr(_f32(x0), C.c_float), _ptr(_f32(u), C.c_float),
+    return float(load().ko_verdict_margin_f64(C.byref(k), _ptr(_f32(x0), C.c_float), _ptr(_f32(u), C.c_float),
                                            _ptr(obs, C.c_float), obs.shape[0]))
 
 

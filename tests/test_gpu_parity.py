@@ -1,0 +1,274 @@
+"""CUDA planner vs the CPU oracle and the reference-made golden vectors.
+
+Integer results (region ids, verdicts, tree parents, node counts, iteration
+counts, goal indices) must be bit-exact; with the same float operation order
+the samples themselves are bit-exact too.  Propagated states are checked
+against the FP64 RK4 oracle with |delta| <= 1e-5 * max(|ref|, scale)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from kgmt_gb300 import workloads as W
+from kgmt_gb300.config import DI_RULE_REFERENCE, double_integrator_single, quadrotor_large
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+DEV = "cuda:0"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from kgmt_gb300._abi import load
+    load()
+
+
+def state_scales(cfg):
+    D = cfg.sample_dim
+    s = np.ones(D)
+    s[:3] = cfg.ws_max - cfg.ws_min
+    if D == 10:
+        s[3:6] = cfg.v_max
+        s[9] = cfg.step_size
+    else:
+        s[3:6] = np.pi
+        s[6:9] = cfg.v_max
+        s[16] = cfg.step_size
+    return s
+
+
+def gpu_propagate(cfg, x0, u, obs):
+    from kgmt_gb300.planner import propagate_samples
+    n, D = x0.shape
+    d_x0 = torch.from_numpy(np.ascontiguousarray(x0, np.float32)).to(DEV)
+    d_u = torch.from_numpy(np.ascontiguousarray(u, np.float32)).to(DEV)
+    d_obs = torch.from_numpy(np.ascontiguousarray(obs, np.float32).reshape(-1, 6)).to(DEV)
+    d_x1 = torch.zeros((n, D), dtype=torch.float32, device=DEV)
+    d_valid = torch.zeros(n, dtype=torch.uint8, device=DEV)
+    d_r1 = torch.zeros(n, dtype=torch.int32, device=DEV)
+    d_r2 = torch.zeros(n, dtype=torch.int32, device=DEV)
+    propagate_samples(cfg, d_x0, d_u, d_obs, d_obs.shape[0], n, d_x1, d_valid, d_r1, d_r2)
+    torch.cuda.synchronize()
+    return d_x1.cpu().numpy(), d_valid.cpu().numpy(), d_r1.cpu().numpy(), d_r2.cpu().numpy()
+
+
+def random_inputs(cfg, n, seed):
+    rng = np.random.Generator(np.random.Philox(key=seed))
+    D = cfg.sample_dim
+    x0 = np.zeros((n, D), np.float32)
+    x0[:, :3] = rng.uniform(0.05, 0.95, (n, 3))
+    if D == 10:
+        x0[:, 3:6] = rng.uniform(-0.3, 0.3, (n, 3))
+    else:
+        x0[:, 3:6] = rng.uniform(-0.6, 0.6, (n, 3))
+        x0[:, 6:9] = rng.uniform(-0.25, 0.25, (n, 3))
+        x0[:, 9:12] = rng.uniform(-1.5, 1.5, (n, 3))
+    u = np.stack([O.sample_uniforms(seed, i, 3) for i in range(n)])
+    return x0, u
+
+
+# ---------------------------------------------------------------------------
+# function level
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("rule", [0, 1])
+def test_propagate_di_bit_exact_vs_oracle(rule):
+    q = W.double_integrator_query(seed=2)
+    cfg = q.config.replace(di_rule=rule)
+    x0, u = random_inputs(cfg, 4096, 11)
+    gx, gv, g1, g2 = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, o1, o2 = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert np.array_equal(gv, ov)
+    assert np.array_equal(gx.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
+
+
+def test_propagate_quad_bit_exact_vs_oracle():
+    q = W.quadrotor_query(seed=2)
+    cfg = q.config
+    x0, u = random_inputs(cfg, 2048, 12)
+    gx, gv, g1, g2 = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, o1, o2 = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert np.array_equal(gv, ov)
+    assert np.array_equal(gx.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
+
+
+@pytest.mark.parametrize("model", ["di", "quad"])
+def test_propagate_within_tolerance_of_fp64(model):
+    q = W.double_integrator_query(seed=3) if model == "di" else W.quadrotor_query(seed=3)
+    cfg = q.config
+    x0, u = random_inputs(cfg, 4096, 13)
+    gx, gv, _, _ = gpu_propagate(cfg, x0, u, q.obstacles)
+    dx, dv = O.propagate_f64(cfg, x0, u, q.obstacles)
+    same = gv == dv
+    mism = np.flatnonzero(~same)
+    # a verdict may flip only where the FP64 trajectory passes within 1e-5 of
+    # a threshold (obstacle face, velocity or workspace bound); such samples
+    # are reported, not failed
+    margins = [O.verdict_margin_f64(cfg, x0[i], u[i], q.obstacles) for i in mism]
+    print(f"{model}: {len(mism)} / {len(gv)} verdicts differ from FP64, all near a threshold: "
+          f"max margin {max(margins) if margins else 0:.2e}")
+    assert all(m < 1e-5 for m in margins)
+    tol = REL_TOL * np.maximum(np.abs(dx), state_scales(cfg))
+    err = np.abs(gx.astype(np.float64) - dx)
+    assert np.all(err[same] <= tol[same]), float((err[same] / tol[same]).max())
+
+
+def test_propagate_matches_reference_golden(golden_dir):
+    g = np.load(golden_dir / "ref_di.npz")
+    cfg = double_integrator_single().replace(di_rule=DI_RULE_REFERENCE)
+    gx, gv, _, _ = gpu_propagate(cfg, g["x0"], g["u"], g["obstacles"])
+    assert np.array_equal(gv, g["valid"])
+    assert np.array_equal(gx.view(np.uint32), g["x1"].view(np.uint32))
+    gq = np.load(golden_dir / "ref_quad.npz")
+    cq = quadrotor_large().replace(min_steps=1, max_steps=15)
+    qx, qv, _, _ = gpu_propagate(cq, gq["x0"], gq["u"], gq["obstacles"])
+    same = qv == gq["valid"]
+    assert same.mean() > 0.99
+    tol = REL_TOL * np.maximum(np.abs(gq["x1"]), state_scales(cq))
+    assert np.all(np.abs(qx - gq["x1"])[same] <= tol[same])
+
+
+# ---------------------------------------------------------------------------
+# whole plans
+# ---------------------------------------------------------------------------
+def plan_gpu(q):
+    from kgmt_gb300.planner import KGMT
+    d_obs = torch.from_numpy(np.ascontiguousarray(q.obstacles, np.float32).reshape(-1, 6)).to(DEV)
+    p = KGMT(q.config)
+    res = p.plan(q.init, q.goal, d_obs, q.obstacles.shape[0])
+    samples, parents, costs = p.copy_tree()
+    path = p.copy_path()
+    p.close()
+    return res, samples, parents, costs, path
+
+
+def assert_same_plan(res, samples, parents, costs, path, ref):
+    for k in ("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn"):
+        assert res[k] == ref[k], (k, res[k], ref[k])
+    assert np.array_equal(parents, ref["parents"])
+    assert np.array_equal(samples.view(np.uint32), ref["samples"].view(np.uint32))
+    assert np.array_equal(costs.view(np.uint32), ref["costs"].view(np.uint32))
+    assert np.array_equal(path.view(np.uint32), ref["path"].view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_plan_double_integrator_bit_exact(seed):
+    q = W.double_integrator_query(seed=seed)
+    out = plan_gpu(q)
+    assert_same_plan(*out, O.plan(q))
+
+
+def test_plan_double_integrator_reference_rule_bit_exact():
+    q = W.double_integrator_query(seed=4)
+    q.config = q.config.replace(di_rule=DI_RULE_REFERENCE)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+def test_plan_quadrotor_small_bit_exact():
+    q = W.quadrotor_query(seed=1, tree_capacity=30_000, max_iterations=25)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+def test_plan_edge_cases():
+    # no obstacles
+    q = W.double_integrator_query(seed=6)
+    q.obstacles = np.zeros((0, 6), np.float32)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+    # tiny tree: capacity exhausted, truncated frontier expansion
+    q = W.double_integrator_query(seed=7)
+    q.config = q.config.replace(tree_capacity=60, max_iterations=50)
+    out = plan_gpu(q)
+    ref = O.plan(q)
+    assert ref["status"] == 3
+    assert_same_plan(*out, ref)
+    # one iteration budget
+    q = W.double_integrator_query(seed=8)
+    q.config = q.config.replace(max_iterations=1)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+    # goal ball around the start: found by the first accepted child
+    q = W.double_integrator_query(seed=9)
+    q.goal = q.init.copy()
+    q.config = q.config.replace(goal_radius=0.2)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+    # many obstacles (global-memory path past the shared-memory stage)
+    q = W.double_integrator_query(seed=10, n_obstacles=1500)
+    q.obstacles[:, 3:] = q.obstacles[:, :3] + 0.01
+    q.config = q.config.replace(tree_capacity=20_000, max_iterations=15)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+# ---------------------------------------------------------------------------
+# batched and served forms
+# ---------------------------------------------------------------------------
+def _batch(queries, block=256, graph=True):
+    from kgmt_gb300.planner import BatchPlanner
+    inits, goals, obs, offs, cnts = W.pack_queries(queries)
+    b = BatchPlanner(len(queries), propagate_block=block, use_graph=graph)
+    res = b.plan([q.config for q in queries], inits, goals, obs, offs, cnts)
+    return b, res
+
+
+def test_batch_matches_oracle_and_plain():
+    qs = W.double_integrator_batch(24, n_obstacles=50, seed=3, tree_capacity=20_000)
+    b, res = _batch(qs)
+    refs = O.plan_batch(qs)
+    for i, (r, ref) in enumerate(zip(res, refs)):
+        for k in ("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn"):
+            assert r[k] == ref[k], (i, k, r[k], ref[k])
+    # the same query alone gives the same tree
+    for i in (0, 7, 23):
+        alone = plan_gpu(qs[i])
+        s, p, c = b.copy_tree(i)
+        n = res[i]["tree_size"]
+        assert np.array_equal(p[:n], alone[2])
+        assert np.array_equal(s[:n].view(np.uint32), alone[1].view(np.uint32))
+
+
+def test_batch_heterogeneous_matches_oracle():
+    qs = W.mixed_batch(24, seed=2, capacity_scale=0.1)
+    for q in qs:
+        q.config = q.config.replace(max_iterations=30)
+    b, res = _batch(qs)
+    refs = O.plan_batch(qs)
+    for i, (r, ref) in enumerate(zip(res, refs)):
+        for k in ("status", "iterations", "tree_size", "goal_index", "samples_drawn"):
+            assert r[k] == ref[k], (i, k, r[k], ref[k])
+
+
+@pytest.mark.parametrize("block", [64, 128, 512])
+def test_block_size_does_not_change_results(block):
+    qs = W.double_integrator_batch(8, seed=5, tree_capacity=20_000)
+    _, base = _batch(qs, 256)
+    _, other = _batch(qs, block, graph=False)
+    assert [(r["tree_size"], r["goal_index"], r["iterations"]) for r in base] == \
+        [(r["tree_size"], r["goal_index"], r["iterations"]) for r in other]
+
+
+def test_server_results_same_alone_and_in_mix():
+    from kgmt_gb300.planner import Server
+    qs = W.double_integrator_batch(12, seed=6, tree_capacity=20_000)
+    refs = O.plan_batch(qs)
+    srv = Server(max_slots=4, memory_budget=1 << 30, iters_per_step=2)
+    tickets = {}
+    pending = list(range(len(qs)))
+    got = {}
+    steps = 0
+    while len(got) < len(qs):
+        # staggered arrivals: two new queries every step
+        for _ in range(2):
+            if pending:
+                i = pending.pop(0)
+                tickets[srv.submit(qs[i].config, qs[i].init, qs[i].goal, qs[i].obstacles)] = i
+        srv.step()
+        for r in srv.poll():
+            got[tickets[r["ticket"]]] = r
+        steps += 1
+        assert steps < 5000
+    for i, ref in enumerate(refs):
+        for k in ("status", "iterations", "tree_size", "goal_index", "samples_drawn"):
+            assert got[i][k] == ref[k], (i, k, got[i][k], ref[k])
