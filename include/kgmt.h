@@ -150,7 +150,20 @@ typedef struct kgmt_batch_options {
     uint32_t iters_per_graph;  /* iterations captured per CUDA graph replay (0: 4) */
     uint32_t propagate_block;  /* 0 = autotuned / default                        */
     uint32_t use_graph;        /* 1 = replay a captured CUDA graph                */
+    uint32_t profile_kernels;  /* 1 = direct launches bracketed by CUDA events    */
 } kgmt_batch_options;
+
+/* counters of the last kgmt_plan_batch* call */
+typedef struct kgmt_batch_stats {
+    uint64_t kernel_launches;     /* kernels this library launched                 */
+    uint64_t steps_executed;      /* RK4 steps over all propagated samples         */
+    uint64_t obstacle_tests;      /* step-box x obstacle-box tests                 */
+    uint64_t samples;             /* samples propagated                            */
+    uint64_t fp32_ops;            /* algorithmic FP32 operations of k_propagate    */
+    uint32_t iterations_launched; /* iterations launched (incl. the no-op tail)    */
+    uint32_t launches_propagate, launches_score, launches_append;
+    float ms_propagate, ms_score, ms_append; /* summed CUDA-event time (profile_kernels) */
+} kgmt_batch_stats;
 
 KGMT_API kgmt_status kgmt_batch_create(const kgmt_batch_options* opt, void* stream, kgmt_batch** out);
 KGMT_API void kgmt_batch_destroy(kgmt_batch* b);
@@ -164,6 +177,7 @@ KGMT_API kgmt_status kgmt_plan_batch(kgmt_batch* b, uint32_t n, const kgmt_confi
 KGMT_API kgmt_status kgmt_plan_batch_device(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* d_inits, const float* d_goals,
                                    const float* d_obstacles, const uint32_t* h_obs_offset, const uint32_t* h_obs_count,
                                    kgmt_result* results);
+KGMT_API kgmt_status kgmt_batch_get_stats(kgmt_batch* b, kgmt_batch_stats* out);
 /* tree of query i of the last batch (host copy) */
 KGMT_API kgmt_status kgmt_batch_copy_tree(kgmt_batch* b, uint32_t i, float* h_samples, int32_t* h_parents, float* h_costs, uint32_t max_nodes);
 KGMT_API kgmt_status kgmt_batch_copy_path(kgmt_batch* b, uint32_t i, float* h_rows, uint32_t max_rows, uint32_t* n_rows);

@@ -48,7 +48,17 @@ class KgmtResult(C.Structure):
 
 class KgmtBatchOptions(C.Structure):
     _fields_ = [("max_queries", C.c_uint32), ("iters_per_graph", C.c_uint32), ("propagate_block", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("profile_kernels", C.c_uint32)]
+
+
+class KgmtBatchStats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_uint64), ("steps_executed", C.c_uint64), ("obstacle_tests", C.c_uint64),
+                ("samples", C.c_uint64), ("fp32_ops", C.c_uint64), ("iterations_launched", C.c_uint32),
+                ("launches_propagate", C.c_uint32), ("launches_score", C.c_uint32), ("launches_append", C.c_uint32),
+                ("ms_propagate", C.c_float), ("ms_score", C.c_float), ("ms_append", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class KgmtServerOptions(C.Structure):
@@ -90,6 +100,7 @@ SIGNATURES = {
     "kgmt_batch_destroy": (None, [_vp]),
     "kgmt_plan_batch": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, _resp]),
     "kgmt_plan_batch_device": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, _resp]),
+    "kgmt_batch_get_stats": (_i32, [_vp, C.POINTER(KgmtBatchStats)]),
     "kgmt_batch_copy_tree": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32]),
     "kgmt_batch_copy_path": (_i32, [_vp, _u32, _vp, _u32, _u32p]),
     "kgmt_batch_autotune": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, _u32p]),

@@ -250,6 +250,7 @@ struct kgmt_batch {
     std::vector<QueryState> states;
     std::vector<QueryParams> params;
     uint32_t n_last = 0;
+    kgmt_batch_stats stats{};
 };
 
 extern "C" kgmt_status kgmt_batch_create(const kgmt_batch_options* opt, void* stream, kgmt_batch** out)
@@ -267,6 +268,7 @@ extern "C" kgmt_status kgmt_batch_create(const kgmt_batch_options* opt, void* st
             delete b;
             return st;
         }
+    b->eng.set_profile(opt->profile_kernels != 0);
     *out = b;
     return KGMT_OK;
 }
@@ -280,6 +282,7 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
 {
     RETURN_IF(n == 0 || n > b->eng.slots(), KGMT_ERR_CAPACITY, "batch: query count exceeds max_queries");
     RETURN_IF(!cfgs || !obs_offset || !obs_count, KGMT_ERR_INVALID_ARG, "batch: NULL argument");
+    b->eng.reset_counters();
     uint64_t boxes = 0;
     uint32_t max_iters = 0;
     size_t total = 0;
@@ -324,6 +327,7 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     uint32_t max_iters = 0;
     for(uint32_t i = 0; i < n; ++i)
         if(cfgs[i].max_iterations > max_iters) max_iters = cfgs[i].max_iterations;
+    const uint32_t it0 = b->eng.iterations_launched();
     CHECK_ST(b->eng.admit(0, n, n, d_inits, d_goals));
     CHECK_ST(b->eng.run_until_done(max_iters));
     CHECK_ST(b->eng.extract_paths(n));
@@ -333,8 +337,34 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     CHECK_ST(b->eng.read_error(&err));
     b->n_last = n;
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "batch: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    // counters of this call
+    kgmt_batch_stats& s = b->stats;
+    std::memset(&s, 0, sizeof(s));
+    s.kernel_launches = b->eng.launches();
+    s.iterations_launched = b->eng.iterations_launched() - it0;
+    for(uint32_t i = 0; i < n; ++i)
+        {
+            const QueryState& q = b->states[i];
+            const uint64_t per_step = cfgs[i].model == KGMT_MODEL_QUADROTOR ? kOpsPerStepQuad : kOpsPerStepDI;
+            s.steps_executed += q.steps;
+            s.obstacle_tests += q.steps * (uint64_t)b->params[i].n_obstacles;
+            s.samples += q.samples_drawn;
+            s.fp32_ops += q.steps * (per_step + (uint64_t)kOpsPerObstacleTest * b->params[i].n_obstacles);
+        }
+    float ms[3];
+    uint32_t cnt[3];
+    CHECK_ST(b->eng.kernel_times(ms, cnt));
+    s.ms_propagate = ms[0], s.ms_score = ms[1], s.ms_append = ms[2];
+    s.launches_propagate = cnt[0], s.launches_score = cnt[1], s.launches_append = cnt[2];
     if(results)
         for(uint32_t i = 0; i < n; ++i) results[i] = to_result(b->states[i], i);
+    return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_batch_get_stats(kgmt_batch* b, kgmt_batch_stats* out)
+{
+    RETURN_IF(!b || !out, KGMT_ERR_INVALID_ARG, "kgmt_batch_get_stats: NULL argument");
+    *out = b->stats;
     return KGMT_OK;
 }
 
@@ -355,6 +385,7 @@ extern "C" kgmt_status kgmt_plan_batch(kgmt_batch* b, uint32_t n, const kgmt_con
         {
             CHECK_ST(cuda_status(cudaMemcpyAsync(raw, h_obstacles, (size_t)boxes * 24, cudaMemcpyHostToDevice, s), "upload obstacles"));
             CHECK_ST(cuda_status(launch_stage_obstacles(raw, region, boxes, s), "stage obstacles"));
+            b->eng.add_launches(1);
         }
     return batch_run(b, n, cfgs, nullptr, nullptr, results);
 }
@@ -370,7 +401,11 @@ extern "C" kgmt_status kgmt_plan_batch_device(kgmt_batch* b, uint32_t n, const k
     uint32_t boxes = 0;
     CHECK_ST(batch_prepare(b, n, cfgs, nullptr, nullptr, h_obs_offset, h_obs_count, &raw_off, &region, &boxes));
     RETURN_IF(boxes > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch_device: obstacles pointer is NULL");
-    if(boxes) CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, region, boxes, b->eng.stream()), "stage obstacles"));
+    if(boxes)
+        {
+            CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, region, boxes, b->eng.stream()), "stage obstacles"));
+            b->eng.add_launches(1);
+        }
     return batch_run(b, n, cfgs, d_inits, d_goals, results);
 }
 

@@ -162,7 +162,7 @@ __device__ __forceinline__ int draw_steps(const QueryParams& P, float u)
 // x0/x1 are sample rows [x y z vx vy vz ax ay az duration].
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
-                                             float* x1)
+                                             float* x1, int& steps_done)
 {
     const float a0 = P.u_min[0] + u[0] * P.u_span[0];
     const float a1 = P.u_min[1] + u[1] * P.u_span[1];
@@ -174,8 +174,10 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* 
     const float a[3] = {a0, a1, a2};
     const bool ref_rule = P.di_rule == KGMT_DI_RULE_REFERENCE;
     bool ok = true;
+    int done = 0;
     for(int i = 0; i < k; ++i)
         {
+            ++done;
             const float q0 = p[0], q1 = p[1], q2 = p[2];
 #pragma unroll
             for(int d = 0; d < 3; ++d)
@@ -207,6 +209,7 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* 
     x1[3] = v[0], x1[4] = v[1], x1[5] = v[2];
     x1[6] = a0, x1[7] = a1, x1[8] = a2;
     x1[9] = h * (float)k;
+    steps_done = done;
     return ok;
 }
 
@@ -244,7 +247,7 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
 }
 
 __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
-                                               float* x1)
+                                               float* x1, int& steps_done)
 {
     const float zc = P.u_min[0] + u[0] * P.u_span[0];
     const float lc = P.u_min[1] + u[1] * P.u_span[1];
@@ -256,8 +259,10 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float
 #pragma unroll
     for(int j = 0; j < 12; ++j) s[j] = x0[j];
     bool ok = true;
+    int done = 0;
     for(int i = 0; i < k; ++i)
         {
+            ++done;
             const float q0 = s[0], q1 = s[1], q2 = s[2];
             quad_ode(P, s, zc, lc, mc, nc, k1);
 #pragma unroll
@@ -291,6 +296,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float
     for(int j = 0; j < 12; ++j) x1[j] = s[j];
     x1[12] = zc, x1[13] = lc, x1[14] = mc, x1[15] = nc;
     x1[16] = h * (float)k;
+    steps_done = done;
     return ok;
 }
 

@@ -337,7 +337,10 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     KGMT_CUDA(cudaMalloc(&d_tile_a_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
     KGMT_CUDA(cudaMalloc(&d_tile_c_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
     KGMT_CUDA(cudaMalloc(&d_tile_old_, sizeof(uint32_t) * slots), "cudaMalloc(tiles)");
-    KGMT_CUDA(cudaMemsetAsync(d_states_, 0, sizeof(QueryState) * slots, stream_), "memset(states)");
+    // empty slots: zeroed params, status bytes 0xFF (kSlotEmpty), so no kernel
+    // treats a slot as running before it is admitted
+    KGMT_CUDA(cudaMemsetAsync(d_params_, 0, sizeof(QueryParams) * slots, stream_), "memset(params)");
+    KGMT_CUDA(cudaMemsetAsync(d_states_, 0xFF, sizeof(QueryState) * slots, stream_), "memset(states)");
     KGMT_CUDA(cudaMemsetAsync(d_tile_a_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_c_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_old_, 0, sizeof(uint32_t) * slots, stream_), "memset");
@@ -398,8 +401,10 @@ kgmt_status Engine::init_slots(uint32_t first, uint32_t count, const float* d_in
         {
             k_set_endpoints<<<(count + 127) / 128, 128, 0, stream_>>>(d_params_, first, count, d_inits, d_goals);
             KGMT_CUDA(cudaGetLastError(), "k_set_endpoints");
+            launches_ += 1;
         }
     KGMT_CUDA(launch_admit(args(), first, count, stream_), "k_admit");
+    launches_ += 1;
     return KGMT_OK;
 }
 
@@ -419,6 +424,7 @@ kgmt_status Engine::set_active(uint32_t n_active)
 kgmt_status Engine::schedule()
 {
     KGMT_CUDA(launch_schedule(args(), stream_), "k_schedule");
+    launches_ += 1;
     return KGMT_OK;
 }
 
@@ -431,12 +437,62 @@ kgmt_status Engine::admit(uint32_t first, uint32_t count, uint32_t n_active, con
     return st;
 }
 
+kgmt_status Engine::record_event(cudaEvent_t* out)
+{
+    if(prof_used_ >= prof_events_.size())
+        {
+            cudaEvent_t e;
+            KGMT_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+            prof_events_.push_back(e);
+        }
+    cudaEvent_t e = prof_events_[prof_used_++];
+    KGMT_CUDA(cudaEventRecord(e, stream_), "cudaEventRecord");
+    if(out) *out = e;
+    return KGMT_OK;
+}
+
 kgmt_status Engine::launch_iteration()
 {
     const LaunchArgs a = args();
-    KGMT_CUDA(launch_propagate(a, (int)prop_block_, grid_a_, stream_), "k_propagate");
-    KGMT_CUDA(launch_score(a, (int)slots_, stream_), "k_score");
-    KGMT_CUDA(launch_append(a, grid_c_, stream_), "k_append");
+    for(int k = 0; k < 3; ++k)
+        {
+            if(profile_)
+                {
+                    kgmt_status st = record_event(nullptr);
+                    if(st != KGMT_OK) return st;
+                    prof_kind_.push_back(k);
+                }
+            if(k == 0) KGMT_CUDA(launch_propagate(a, (int)prop_block_, grid_a_, stream_), "k_propagate");
+            else if(k == 1) KGMT_CUDA(launch_score(a, (int)slots_, stream_), "k_score");
+            else KGMT_CUDA(launch_append(a, grid_c_, stream_), "k_append");
+            if(profile_)
+                {
+                    kgmt_status st = record_event(nullptr);
+                    if(st != KGMT_OK) return st;
+                }
+        }
+    launches_ += 3;
+    return KGMT_OK;
+}
+
+void Engine::reset_counters()
+{
+    launches_ = 0;
+    prof_used_ = 0;
+    prof_kind_.clear();
+}
+
+kgmt_status Engine::kernel_times(float ms[3], uint32_t n[3])
+{
+    for(int k = 0; k < 3; ++k) ms[k] = 0.0f, n[k] = 0;
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    for(size_t i = 0; i < prof_kind_.size(); ++i)
+        {
+            float t = 0.0f;
+            KGMT_CUDA(cudaEventElapsedTime(&t, prof_events_[2 * i], prof_events_[2 * i + 1]), "cudaEventElapsedTime");
+            ms[prof_kind_[i]] += t;
+            n[prof_kind_[i]] += 1;
+        }
     return KGMT_OK;
 }
 
@@ -445,7 +501,9 @@ kgmt_status Engine::build_graph()
     cudaGraph_t g = nullptr;
     KGMT_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     kgmt_status st = KGMT_OK;
+    const uint64_t saved = launches_;
     for(uint32_t i = 0; i < iters_per_graph_ && st == KGMT_OK; ++i) st = launch_iteration();
+    launches_ = saved;
     cudaError_t e = cudaStreamEndCapture(stream_, &g);
     if(st != KGMT_OK)
         {
@@ -460,7 +518,7 @@ kgmt_status Engine::build_graph()
 
 kgmt_status Engine::launch_unit()
 {
-    if(use_graph_)
+    if(use_graph_ && !profile_)
         {
             if(!graph_)
                 {
@@ -468,6 +526,7 @@ kgmt_status Engine::launch_unit()
                     if(st != KGMT_OK) return st;
                 }
             KGMT_CUDA(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
+            launches_ += 3ull * iters_per_graph_;
         }
     else
         {
@@ -524,6 +583,7 @@ kgmt_status Engine::read_states(uint32_t first, uint32_t count, QueryState* out)
 kgmt_status Engine::extract_paths(uint32_t n_active)
 {
     KGMT_CUDA(launch_paths(args(), n_active, stream_), "k_paths");
+    launches_ += 1;
     return KGMT_OK;
 }
 

@@ -88,8 +88,17 @@ class Engine {
     uint32_t prop_block() const { return prop_block_; }
     uint32_t iterations_launched() const { return iters_launched_; }
 
+    // per-kernel CUDA-event timing (direct launches instead of the graph)
+    void set_profile(bool on) { profile_ = on; }
+    void reset_counters();
+    void add_launches(uint64_t n) { launches_ += n; }
+    uint64_t launches() const { return launches_; }
+    // sums the event pairs recorded since reset_counters (call after a sync)
+    kgmt_status kernel_times(float ms[3], uint32_t n[3]);
+
    private:
     kgmt_status launch_iteration();
+    kgmt_status record_event(cudaEvent_t* out);
     kgmt_status launch_unit();
     kgmt_status build_graph();
 
@@ -111,6 +120,11 @@ class Engine {
     cudaGraphExec_t graph_ = nullptr;
     std::vector<QueryParams> h_params_;
     uint32_t iters_launched_ = 0;
+    uint64_t launches_ = 0;
+    bool profile_ = false;
+    std::vector<cudaEvent_t> prof_events_;  // pool, pairs (start, stop)
+    std::vector<int> prof_kind_;            // kernel of each pair
+    size_t prof_used_ = 0;
 };
 
 }  // namespace kgmt

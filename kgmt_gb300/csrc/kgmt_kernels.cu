@@ -285,6 +285,7 @@ __global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32
             st.w_new = kRootRepeat;
             st.goal_cand = INT_MAX;
             st.goal_index = -1;
+            st.steps = 0;
             st.t_start = globaltimer();
             plan_samples(p, st);
             S[q] = st;
@@ -311,7 +312,7 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
     constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
     constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
     const unsigned full = 0xffffffffu;
-    int r1 = -1, r2 = 0;
+    int r1 = -1, r2 = 0, steps = 0;
     bool ok = false, acc = false;
     if(live)
         {
@@ -325,8 +326,8 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
             const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
             const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
             const float u[8] = {u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), u01(b.y), u01(b.z), u01(b.w)};
-            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1);
-            else ok = propagate_di(p, x0, u, obs, n_obs, x1);
+            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1, steps);
+            else ok = propagate_di(p, x0, u, obs, n_obs, x1, steps);
             const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
             r1 = cid.r1;
             r2 = cid.r2;
@@ -359,7 +360,12 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
             if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.valid[r1], __popc(peers));
         }
     const unsigned acc_mask = __ballot_sync(full, acc);
-    if((threadIdx.x & 31) == 0 && acc_mask) atomicAdd(&st->n_next, __popc(acc_mask));
+    const unsigned warp_steps = __reduce_add_sync(full, (unsigned)steps);
+    if((threadIdx.x & 31) == 0)
+        {
+            if(acc_mask) atomicAdd(&st->n_next, __popc(acc_mask));
+            if(warp_steps) atomicAdd(&st->steps, (unsigned long long)warp_steps);
+        }
 }
 
 template <int NT>
@@ -767,7 +773,9 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
     float a[kMaxSampleDim], b[kMaxSampleDim], u[8];
     for(int j = 0; j < D; ++j) a[j] = x0[(size_t)s * D + j];
     for(int j = 0; j < 8; ++j) u[j] = uni[(size_t)s * 8 + j];
-    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b) : propagate_di(p, a, u, s_obs, n_obs, b);
+    int steps = 0;
+    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b, steps)
+                                              : propagate_di(p, a, u, s_obs, n_obs, b, steps);
     for(int j = 0; j < D; ++j) x1[(size_t)s * D + j] = b[j];
     valid[s] = ok ? 1 : 0;
     const CellIds c = cell_ids(p, b[0], b[1], b[2]);

@@ -24,6 +24,15 @@ constexpr int kSparseValidLimit = 10;   // KGMT.cu:336
 constexpr int kSmemObstacles = 1024;    // boxes staged in shared memory per block
 constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a device-side wait gives up
 
+constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-admitted slot
+
+// static FP32 operation counts per RK4 step, from the code in kgmt_device.cuh
+// (multiplies, adds, divides, compares; the quadrotor's portable sine/cosine
+// counted as the float operations they are made of)
+constexpr uint32_t kOpsPerStepDI = 81;
+constexpr uint32_t kOpsPerStepQuad = 974;
+constexpr uint32_t kOpsPerObstacleTest = 6;
+
 // error bits in Sched::error
 constexpr uint32_t kErrLookbackTimeout = 1u;
 constexpr uint32_t kErrCopyTimeout = 2u;
@@ -93,8 +102,9 @@ struct QueryState {
     float score_total;
     uint32_t samples_drawn;
     uint32_t path_len;
-    unsigned long long t_start;  // %globaltimer_lo at admission (ns)
+    unsigned long long t_start;  // %globaltimer at admission (ns)
     unsigned long long t_end;
+    unsigned long long steps;    // RK4 steps executed over all samples
 };
 
 struct Sched {

@@ -117,9 +117,10 @@ class BatchPlanner:
     """Many independent queries in one device-resident launch chain."""
 
     def __init__(self, max_queries: int, iters_per_graph: int = 4, propagate_block: int = 256, use_graph: bool = True,
-                 stream: int | None = None):
+                 stream: int | None = None, profile_kernels: bool = False):
         self._lib = load()
-        opt = KgmtBatchOptions(max_queries, iters_per_graph, propagate_block, 1 if use_graph else 0)
+        opt = KgmtBatchOptions(max_queries, iters_per_graph, propagate_block, 1 if use_graph else 0,
+                               1 if profile_kernels else 0)
         h = C.c_void_p()
         check(self._lib.kgmt_batch_create(C.byref(opt), stream, C.byref(h)))
         self._h = h
@@ -164,6 +165,11 @@ class BatchPlanner:
         self._n = n
         self._cfgs = list(cfgs)
         return res
+
+    def stats(self) -> dict:
+        s = _abi.KgmtBatchStats()
+        check(self._lib.kgmt_batch_get_stats(self._h, C.byref(s)))
+        return s.as_dict()
 
     def copy_tree(self, i: int):
         r_cfg = self._cfgs[i]
