@@ -110,7 +110,7 @@ extern "C" kgmt_status kgmt_config_validate(const kgmt_config* cfg)
 extern "C" size_t kgmt_query_bytes(const kgmt_config* cfg, uint32_t n_obstacles)
 {
     if(!cfg || validate_config(*cfg) != KGMT_OK) return 0;
-    return layout_of(*cfg, n_obstacles).total;
+    return layout_of(*cfg, n_obstacles, true).total;
 }
 
 static bool is_device_pointer(const void* p)
@@ -145,7 +145,7 @@ extern "C" kgmt_status kgmt_create(const kgmt_config* cfg, void* stream, kgmt_pl
     RETURN_IF(!p, KGMT_ERR_OOM, "kgmt_create: host allocation failed");
     p->cfg = *cfg;
     kgmt_status st = p->eng.init(1, (cudaStream_t)stream, 256, 4, true);
-    if(st == KGMT_OK) st = p->arena.reserve(layout_of(*cfg, 0).total);
+    if(st == KGMT_OK) st = p->arena.reserve(layout_of(*cfg, 0, true).total);
     if(st != KGMT_OK)
         {
             delete p;
@@ -165,7 +165,7 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
     RETURN_IF(n_obstacles > 0 && !is_device_pointer(d_obstacles), KGMT_ERR_INVALID_ARG,
               "kgmt_plan: obstacles must be a device pointer (as in KGMT::plan)");
     p->planned = false;
-    const QueryLayout L = layout_of(p->cfg, n_obstacles);
+    const QueryLayout L = layout_of(p->cfg, n_obstacles, true);
     p->arena.reset();
     CHECK_ST(p->arena.reserve(L.total));
     size_t off = 0;
@@ -290,7 +290,7 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
     for(uint32_t i = 0; i < n; ++i)
         {
             CHECK_ST(validate_config(cfgs[i]));
-            L[i] = layout_of(cfgs[i], 0);
+            L[i] = layout_of(cfgs[i], obs_count[i], false);
             total += L[i].total;
             uint64_t end = (uint64_t)obs_offset[i] + obs_count[i];
             if(end > boxes) boxes = end;
@@ -347,9 +347,10 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
             const QueryState& q = b->states[i];
             const uint64_t per_step = cfgs[i].model == KGMT_MODEL_QUADROTOR ? kOpsPerStepQuad : kOpsPerStepDI;
             s.steps_executed += q.steps;
-            s.obstacle_tests += q.steps * (uint64_t)b->params[i].n_obstacles;
+            s.obstacle_tests += q.tests;
             s.samples += q.samples_drawn;
-            s.fp32_ops += q.steps * (per_step + (uint64_t)kOpsPerObstacleTest * b->params[i].n_obstacles);
+            const uint64_t lookup = b->params[i].n_obstacles ? kOpsPerGridLookup : 0;
+            s.fp32_ops += q.steps * (per_step + lookup) + q.tests * kOpsPerObstacleTest;
         }
     float ms[3];
     uint32_t cnt[3];
@@ -514,7 +515,7 @@ extern "C" kgmt_status kgmt_server_submit(kgmt_server* s, const kgmt_config* cfg
     RETURN_IF(!s || !cfg || !h_init || !h_goal, KGMT_ERR_INVALID_ARG, "kgmt_server_submit: NULL argument");
     RETURN_IF(n_obstacles > 0 && !h_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_server_submit: obstacles pointer is NULL");
     CHECK_ST(validate_config(*cfg));
-    const QueryLayout L = layout_of(*cfg, n_obstacles);
+    const QueryLayout L = layout_of(*cfg, n_obstacles, true);
     RETURN_IF(L.total + (size_t)n_obstacles * 24 + 256 > s->arena.capacity(), KGMT_ERR_OOM,
               "kgmt_server_submit: query larger than the memory budget");
     PendingQuery q;
@@ -545,7 +546,7 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
             if(slot >= s->slots.size()) break;
             PendingQuery& q = s->queue.front();
             const uint32_t n_obs = (uint32_t)(q.obstacles.size() / 6);
-            const QueryLayout L = layout_of(q.cfg, n_obs);
+            const QueryLayout L = layout_of(q.cfg, n_obs, true);
             const size_t raw_at = (L.total + 255) & ~size_t(255);
             size_t off = 0;
             if(!s->arena.alloc(raw_at + (size_t)n_obs * 24 + 256, &off)) break;  // wait for memory
@@ -634,7 +635,7 @@ extern "C" kgmt_status kgmt_propagate_samples(const kgmt_config* cfg, const floa
             set_error("no CUDA device");
             return KGMT_ERR_NO_DEVICE;
         }
-    const QueryLayout L = layout_of(*cfg, 0);
+    const QueryLayout L = layout_of(*cfg, 0, false);
     QueryParams p = make_params(*cfg, nullptr, nullptr, nullptr, L, nullptr, n_obstacles);
     return cuda_status(
       launch_propagate_samples(p, d_x0, d_uniforms, d_obstacles, n_obstacles, n, d_x1, d_valid, d_r1, d_r2, (cudaStream_t)stream),

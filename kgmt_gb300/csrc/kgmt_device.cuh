@@ -130,20 +130,63 @@ __device__ __forceinline__ float goal_distance(float x, float y, float z, const 
 // Separated iff bbMax <= obsMin or obsMax <= bbMin on some axis; touching is
 // free.  Returns true when the step box hits no obstacle.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool step_free(const float4* __restrict__ obs, uint32_t n_obs, float ax, float ay, float az, float bx,
-                                          float by, float bz)
+struct PropCount {
+    int steps = 0;       // RK4 steps executed
+    uint32_t tests = 0;  // step-box x box tests
+};
+
+__device__ __forceinline__ bool box_hit(const float4* __restrict__ obs, uint32_t o, float lx, float ly, float lz, float hx, float hy,
+                                        float hz)
 {
+    const float4 mn = obs[2 * o];
+    const float4 mx = obs[2 * o + 1];
+    const bool sep = (hx <= mn.x) | (mx.x <= lx) | (hy <= mn.y) | (mx.y <= ly) | (hz <= mn.z) | (mx.z <= lz);
+    return !sep;
+}
+
+// Cell coordinate on the obstacle grid; monotone in x (every float operation
+// is), so a point inside both a box and the step box lies in a cell both
+// cell ranges contain -- culling by cells never drops a hit.
+__device__ __forceinline__ int grid_cell(const QueryParams& P, float x)
+{
+    return cell_index(((float)P.grid_dim * (x - P.ws_min)) / P.ws_range, (int)P.grid_dim);
+}
+
+// true when the step box [a, b] (per-axis min/max) hits no obstacle
+__device__ __forceinline__ bool step_free(const QueryParams& P, const float4* __restrict__ obs, uint32_t n_obs, float ax, float ay,
+                                          float az, float bx, float by, float bz, PropCount& cnt)
+{
+    if(n_obs == 0) return true;
     const float lx = ax > bx ? bx : ax, hx = ax > bx ? ax : bx;
     const float ly = ay > by ? by : ay, hy = ay > by ? ay : by;
     const float lz = az > bz ? bz : az, hz = az > bz ? az : bz;
-    bool hit = false;
-    for(uint32_t o = 0; o < n_obs; ++o)
+    const uint32_t* __restrict__ gs = P.grid_start;
+    if(gs != nullptr && __ldg(gs + kGridCells + 1) == 1u)
         {
-            const float4 mn = obs[2 * o];
-            const float4 mx = obs[2 * o + 1];
-            const bool sep = (hx <= mn.x) | (mx.x <= lx) | (hy <= mn.y) | (mx.y <= ly) | (hz <= mn.z) | (mx.z <= lz);
-            hit |= !sep;
+            const int x0 = grid_cell(P, lx), x1 = grid_cell(P, hx);
+            const int y0 = grid_cell(P, ly), y1 = grid_cell(P, hy);
+            const int z0 = grid_cell(P, lz), z1 = grid_cell(P, hz);
+            if((uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1)) <= kGridMaxVisit)
+                {
+                    const int G = (int)P.grid_dim;
+                    for(int cx = x0; cx <= x1; ++cx)
+                        for(int cy = y0; cy <= y1; ++cy)
+                            for(int cz = z0; cz <= z1; ++cz)
+                                {
+                                    const int c = (cx * G + cy) * G + cz;
+                                    const uint32_t e = __ldg(gs + c + 1);
+                                    for(uint32_t j = __ldg(gs + c); j < e; ++j)
+                                        {
+                                            ++cnt.tests;
+                                            if(box_hit(obs, __ldg(P.grid_items + j), lx, ly, lz, hx, hy, hz)) return false;
+                                        }
+                                }
+                    return true;
+                }
         }
+    bool hit = false;
+    for(uint32_t o = 0; o < n_obs; ++o) hit |= box_hit(obs, o, lx, ly, lz, hx, hy, hz);
+    cnt.tests += n_obs;
     return !hit;
 }
 
@@ -162,7 +205,7 @@ __device__ __forceinline__ int draw_steps(const QueryParams& P, float u)
 // x0/x1 are sample rows [x y z vx vy vz ax ay az duration].
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
-                                             float* x1, int& steps_done)
+                                             float* x1, PropCount& cnt)
 {
     const float a0 = P.u_min[0] + u[0] * P.u_span[0];
     const float a1 = P.u_min[1] + u[1] * P.u_span[1];
@@ -199,7 +242,7 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* 
                     ok = false;
                     break;
                 }
-            if(!step_free(obs, n_obs, q0, q1, q2, p[0], p[1], p[2]))
+            if(!step_free(P, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], cnt))
                 {
                     ok = false;
                     break;
@@ -209,7 +252,7 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* 
     x1[3] = v[0], x1[4] = v[1], x1[5] = v[2];
     x1[6] = a0, x1[7] = a1, x1[8] = a2;
     x1[9] = h * (float)k;
-    steps_done = done;
+    cnt.steps = done;
     return ok;
 }
 
@@ -247,7 +290,7 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
 }
 
 __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
-                                               float* x1, int& steps_done)
+                                               float* x1, PropCount& cnt)
 {
     const float zc = P.u_min[0] + u[0] * P.u_span[0];
     const float lc = P.u_min[1] + u[1] * P.u_span[1];
@@ -286,7 +329,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float
                     ok = false;
                     break;
                 }
-            if(!step_free(obs, n_obs, q0, q1, q2, s[0], s[1], s[2]))
+            if(!step_free(P, obs, n_obs, q0, q1, q2, s[0], s[1], s[2], cnt))
                 {
                     ok = false;
                     break;
@@ -296,7 +339,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float
     for(int j = 0; j < 12; ++j) x1[j] = s[j];
     x1[12] = zc, x1[13] = lc, x1[14] = mc, x1[15] = nc;
     x1[16] = h * (float)k;
-    steps_done = done;
+    cnt.steps = done;
     return ok;
 }
 

@@ -147,9 +147,10 @@ static size_t aligned(size_t& cur, size_t bytes)
     return off;
 }
 
-QueryLayout layout_of(const kgmt_config& c, uint32_t inline_obstacles)
+QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_obstacles)
 {
     QueryLayout L{};
+    L.grid_budget = n_obstacles ? std::max<uint32_t>(8192u, 32u * n_obstacles) : 0u;
     const size_t T = c.tree_capacity, D = sample_dim_of(c.model);
     const size_t R1 = (size_t)c.coarse_len * c.coarse_len * c.coarse_len;
     L.tiles_per_chain = (uint32_t)((T + kTileC - 1) / kTileC + 1);
@@ -172,7 +173,9 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t inline_obstacles)
     L.tiles_old = aligned(cur, (size_t)L.tiles_per_chain * 8);
     L.tiles_slot = aligned(cur, (size_t)L.tiles_per_chain * 8);
     L.path = aligned(cur, ((size_t)c.max_iterations + 2) * D * 4);
-    L.obstacles = aligned(cur, (size_t)inline_obstacles * 32);
+    L.grid_start = aligned(cur, n_obstacles ? ((size_t)kGridCells + 2) * 4 : 0);
+    L.grid_items = aligned(cur, (size_t)L.grid_budget * 2);
+    L.obstacles = aligned(cur, inline_obstacles ? (size_t)n_obstacles * 32 : 0);
     L.total = cur;
     return L;
 }
@@ -240,6 +243,15 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
         for(uint32_t i = 0; i < D; ++i) p.init[i] = init[i];
     p.n_obstacles = n_obstacles;
     p.tiles_per_chain = L.tiles_per_chain;
+    p.grid_dim = kGridDim;
+    p.grid_budget = L.grid_budget;
+    if(chunk == nullptr)  // parameters only (function-level propagation): no buffers, no grid
+        {
+            p.obstacles = obstacles;
+            return p;
+        }
+    p.grid_start = n_obstacles ? (uint32_t*)(chunk + L.grid_start) : nullptr;
+    p.grid_items = (uint16_t*)(chunk + L.grid_items);
     p.tree = (float*)(chunk + L.tree);
     p.parent = (int32_t*)(chunk + L.parent);
     p.cost = (float*)(chunk + L.cost);
@@ -404,7 +416,7 @@ kgmt_status Engine::init_slots(uint32_t first, uint32_t count, const float* d_in
             launches_ += 1;
         }
     KGMT_CUDA(launch_admit(args(), first, count, stream_), "k_admit");
-    launches_ += 1;
+    launches_ += 2;  // k_admit + k_build_grid
     return KGMT_OK;
 }
 

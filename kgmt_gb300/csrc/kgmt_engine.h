@@ -43,13 +43,16 @@ class DeviceArena {
 
 struct QueryLayout {
     size_t tree, parent, cost, node_r1, rep_old, rep_new, us, up, ur1, uflag;
-    size_t counter, valid, score, marks, newmarks, tiles_old, tiles_slot, path, obstacles;
+    size_t counter, valid, score, marks, newmarks, tiles_old, tiles_slot, path, grid_start, grid_items, obstacles;
     size_t total;
     uint32_t tiles_per_chain;
+    uint32_t grid_budget;
 };
 
 kgmt_status validate_config(const kgmt_config& c);
-QueryLayout layout_of(const kgmt_config& c, uint32_t inline_obstacles);
+// buffers of one query with n_obstacles boxes; the boxes themselves are
+// placed in the chunk only when inline_obstacles (batches share one region)
+QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_obstacles);
 // derived constants in float exactly as the kernels expect them; buffers
 // point into `base + chunk_offset`; obstacles at `obstacles` (device)
 QueryParams make_params(const kgmt_config& c, const float* init, const float* goal, char* chunk, const QueryLayout& L, float4* obstacles,

@@ -151,27 +151,70 @@ constexpr unsigned long long kStAgg = 1ull << 62;
 constexpr unsigned long long kStIncl = 2ull << 62;
 constexpr unsigned long long kValMask = (1ull << 62) - 1;
 
-__device__ unsigned long long lookback(unsigned long long* tiles, int lt, uint32_t* error)
+// Called by one full warp; lane i inspects predecessor lt-1-i, 32 at a time,
+// until the nearest inclusive prefix; every nearer predecessor must have
+// published at least its aggregate.  Returns the exclusive prefix on all lanes.
+__device__ unsigned long long lookback_warp(unsigned long long* tiles, int lt, uint32_t* error)
 {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     unsigned long long prefix = 0;
-    for(int j = lt - 1; j >= 0; --j)
+    int base = lt - 1;
+    uint32_t spins = 0;
+    while(base >= 0)
         {
-            unsigned long long w = ld_volatile_u64(&tiles[j]);
-            uint32_t spins = 0;
-            while((w >> 62) == 0)
+            const int j = base - lane;
+            const unsigned long long w = j >= 0 ? ld_volatile_u64(&tiles[j]) : kStIncl;  // before tile 0: inclusive 0
+            const unsigned st = (unsigned)(w >> 62);
+            const unsigned incl = __ballot_sync(full, st == 2u);
+            const unsigned not_ready = __ballot_sync(full, st == 0u);
+            const int stop = incl ? __ffs(incl) - 1 : 31;  // nearest inclusive lane (or the whole window)
+            const unsigned upto = stop == 31 ? full : ((2u << stop) - 1u);
+            if(not_ready & upto)
                 {
                     if(++spins > kSpinLimit)
                         {
-                            atomicOr(error, kErrLookbackTimeout);
+                            if(lane == 0) atomicOr(error, kErrLookbackTimeout);
                             return prefix;
                         }
                     __nanosleep(32);
-                    w = ld_volatile_u64(&tiles[j]);
+                    continue;
                 }
-            prefix += w & kValMask;
-            if((w >> 62) == 2) break;
+            unsigned long long v = lane <= stop ? (w & kValMask) : 0ull;
+#pragma unroll
+            for(int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(full, v, o);
+            prefix += v;
+            if(incl) break;
+            base -= 32;
         }
     return prefix;
+}
+
+// Tile lt of a chain with block aggregate `agg`: publishes the aggregate,
+// resolves the exclusive prefix (warp 0), publishes the inclusive prefix and
+// leaves the exclusive prefix in *s_prefix.  Block-uniform call; the caller
+// synchronises before reading *s_prefix.
+__device__ __forceinline__ void publish_and_lookback(unsigned long long* tiles, uint32_t lt, unsigned long long agg,
+                                                     unsigned long long* s_prefix, uint32_t* error)
+{
+    if(threadIdx.x >= 32) return;
+    if(lt == 0)
+        {
+            if(threadIdx.x == 0)
+                {
+                    st_volatile_u64(&tiles[0], kStIncl | agg);
+                    *s_prefix = 0;
+                }
+            return;
+        }
+    if(threadIdx.x == 0) st_volatile_u64(&tiles[lt], kStAgg | agg);
+    __syncwarp();
+    const unsigned long long prefix = lookback_warp(tiles, (int)lt, error);
+    if(threadIdx.x == 0)
+        {
+            st_volatile_u64(&tiles[lt], kStIncl | (prefix + agg));
+            *s_prefix = prefix;
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -286,9 +329,85 @@ __global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32
             st.goal_cand = INT_MAX;
             st.goal_index = -1;
             st.steps = 0;
+            st.tests = 0;
             st.t_start = globaltimer();
             plan_samples(p, st);
             S[q] = st;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// obstacle grid of one query per block: count boxes per cell, scan, fill.
+// A box is listed in every cell of [cell(min), cell(max)] per axis (ordered,
+// so an inverted box is still covered).  NaN coordinates, more boxes than
+// 16-bit indices hold, or more entries than the budget leave the grid marked
+// unusable and the propagate kernel tests every box.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restrict__ P, uint32_t first, uint32_t count)
+{
+    __shared__ uint32_t cnt[kGridCells];
+    __shared__ uint32_t scratch[34];
+    __shared__ int s_bad;
+    if(blockIdx.x >= count) return;
+    const QueryParams& p = P[first + blockIdx.x];
+    if(p.grid_start == nullptr) return;
+    const uint32_t n = p.n_obstacles;
+    for(uint32_t i = threadIdx.x; i < kGridCells; i += blockDim.x) cnt[i] = 0;
+    if(threadIdx.x == 0) s_bad = n > kMaxObstacles ? 1 : 0;
+    __syncthreads();
+    const int G = (int)p.grid_dim;
+    for(uint32_t o = threadIdx.x; o < n && !s_bad; o += blockDim.x)
+        {
+            const float4 a = p.obstacles[2 * o], b = p.obstacles[2 * o + 1];
+            if(isnan(a.x) || isnan(a.y) || isnan(a.z) || isnan(b.x) || isnan(b.y) || isnan(b.z))
+                {
+                    s_bad = 1;
+                    break;
+                }
+            const int x0 = grid_cell(p, fminf(a.x, b.x)), x1 = grid_cell(p, fmaxf(a.x, b.x));
+            const int y0 = grid_cell(p, fminf(a.y, b.y)), y1 = grid_cell(p, fmaxf(a.y, b.y));
+            const int z0 = grid_cell(p, fminf(a.z, b.z)), z1 = grid_cell(p, fmaxf(a.z, b.z));
+            for(int cx = x0; cx <= x1; ++cx)
+                for(int cy = y0; cy <= y1; ++cy)
+                    for(int cz = z0; cz <= z1; ++cz) atomicAdd(&cnt[(cx * G + cy) * G + cz], 1u);
+        }
+    __syncthreads();
+    // exclusive scan: thread t owns cells [16 t, 16 t + 16)
+    constexpr int PER = kGridCells / 256;
+    uint32_t local = 0;
+    if(threadIdx.x < 256)
+        for(int i = 0; i < PER; ++i) local += cnt[threadIdx.x * PER + i];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan<256>(local, scratch, &total);
+    for(int i = 0; i < PER; ++i)
+        {
+            const uint32_t c = threadIdx.x * PER + i;
+            const uint32_t k = cnt[c];
+            p.grid_start[c] = run;
+            cnt[c] = run;  // becomes the fill cursor
+            run += k;
+        }
+    const bool usable = !s_bad && total <= p.grid_budget;
+    if(threadIdx.x == 0)
+        {
+            p.grid_start[kGridCells] = total;
+            p.grid_start[kGridCells + 1] = usable ? 1u : 0u;
+        }
+    __syncthreads();
+    if(!usable) return;
+    for(uint32_t o = threadIdx.x; o < n; o += blockDim.x)
+        {
+            const float4 a = p.obstacles[2 * o], b = p.obstacles[2 * o + 1];
+            const int x0 = grid_cell(p, fminf(a.x, b.x)), x1 = grid_cell(p, fmaxf(a.x, b.x));
+            const int y0 = grid_cell(p, fminf(a.y, b.y)), y1 = grid_cell(p, fmaxf(a.y, b.y));
+            const int z0 = grid_cell(p, fminf(a.z, b.z)), z1 = grid_cell(p, fmaxf(a.z, b.z));
+            for(int cx = x0; cx <= x1; ++cx)
+                for(int cy = y0; cy <= y1; ++cy)
+                    for(int cz = z0; cz <= z1; ++cz)
+                        {
+                            const uint32_t pos = atomicAdd(&cnt[(cx * G + cy) * G + cz], 1u);
+                            p.grid_items[pos] = (uint16_t)o;
+                        }
         }
 }
 
@@ -312,7 +431,8 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
     constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
     constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
     const unsigned full = 0xffffffffu;
-    int r1 = -1, r2 = 0, steps = 0;
+    int r1 = -1, r2 = 0;
+    PropCount cnt;
     bool ok = false, acc = false;
     if(live)
         {
@@ -326,8 +446,8 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
             const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
             const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
             const float u[8] = {u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), u01(b.y), u01(b.z), u01(b.w)};
-            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1, steps);
-            else ok = propagate_di(p, x0, u, obs, n_obs, x1, steps);
+            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1, cnt);
+            else ok = propagate_di(p, x0, u, obs, n_obs, x1, cnt);
             const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
             r1 = cid.r1;
             r2 = cid.r2;
@@ -360,11 +480,13 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
             if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.valid[r1], __popc(peers));
         }
     const unsigned acc_mask = __ballot_sync(full, acc);
-    const unsigned warp_steps = __reduce_add_sync(full, (unsigned)steps);
+    const unsigned warp_steps = __reduce_add_sync(full, (unsigned)cnt.steps);
+    const unsigned warp_tests = __reduce_add_sync(full, cnt.tests);
     if((threadIdx.x & 31) == 0)
         {
             if(acc_mask) atomicAdd(&st->n_next, __popc(acc_mask));
             if(warp_steps) atomicAdd(&st->steps, (unsigned long long)warp_steps);
+            if(warp_tests) atomicAdd(&st->tests, (unsigned long long)warp_tests);
         }
 }
 
@@ -607,20 +729,8 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                         }
                     uint32_t agg;
                     const uint32_t excl = block_exclusive_scan<kAppendThreads>(cnt, scratch, &agg);
-                    if(threadIdx.x == 0)
-                        {
-                            unsigned long long prefix = 0;
-                            if(lt == 0) st_volatile_u64(&p.tiles_old[0], kStIncl | agg);
-                            else
-                                {
-                                    st_volatile_u64(&p.tiles_old[lt], kStAgg | agg);
-                                    prefix = lookback(p.tiles_old, (int)lt, &sched->error);
-                                    __threadfence();
-                                    st_volatile_u64(&p.tiles_old[lt], kStIncl | (prefix + agg));
-                                }
-                            s_prefix = prefix;
-                            atomicAdd(&st.react_total, agg);
-                        }
+                    publish_and_lookback(p.tiles_old, lt, agg, &s_prefix, &sched->error);
+                    if(threadIdx.x == 0) atomicAdd(&st.react_total, agg);
                     __syncthreads();
                     uint32_t pos = (uint32_t)s_prefix + excl;
 #pragma unroll
@@ -650,19 +760,10 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     uint32_t agg;
                     const uint32_t excl = block_exclusive_scan<kAppendThreads>((ca << 16) | cw, scratch, &agg);
                     const uint32_t agg_a = agg >> 16, agg_w = agg & 0xffffu;
+                    const unsigned long long val = ((unsigned long long)agg_a << 32) | agg_w;
+                    publish_and_lookback(p.tiles_slot, lts, val, &s_prefix, &sched->error);
                     if(threadIdx.x == 0)
                         {
-                            const unsigned long long val = ((unsigned long long)agg_a << 32) | agg_w;
-                            unsigned long long prefix = 0;
-                            if(lts == 0) st_volatile_u64(&p.tiles_slot[0], kStIncl | val);
-                            else
-                                {
-                                    st_volatile_u64(&p.tiles_slot[lts], kStAgg | val);
-                                    prefix = lookback(p.tiles_slot, (int)lts, &sched->error);
-                                    __threadfence();
-                                    st_volatile_u64(&p.tiles_slot[lts], kStIncl | (prefix + val));
-                                }
-                            s_prefix = prefix;
                             atomicAdd(&st.acc_total, agg_a);
                             atomicAdd(&st.w_total, agg_w);
                         }
@@ -773,9 +874,9 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
     float a[kMaxSampleDim], b[kMaxSampleDim], u[8];
     for(int j = 0; j < D; ++j) a[j] = x0[(size_t)s * D + j];
     for(int j = 0; j < 8; ++j) u[j] = uni[(size_t)s * 8 + j];
-    int steps = 0;
-    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b, steps)
-                                              : propagate_di(p, a, u, s_obs, n_obs, b, steps);
+    PropCount cnt;
+    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b, cnt)
+                                              : propagate_di(p, a, u, s_obs, n_obs, b, cnt);
     for(int j = 0; j < D; ++j) x1[(size_t)s * D + j] = b[j];
     valid[s] = ok ? 1 : 0;
     const CellIds c = cell_ids(p, b[0], b[1], b[2]);
@@ -841,6 +942,9 @@ cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cu
 {
     if(count == 0) return cudaSuccess;
     k_admit<<<count, 256, 0, s>>>(a.params, a.states, first, count);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return e;
+    k_build_grid<<<count, 256, 0, s>>>(a.params, first, count);
     return cudaGetLastError();
 }
 

@@ -32,6 +32,12 @@ constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-a
 constexpr uint32_t kOpsPerStepDI = 81;
 constexpr uint32_t kOpsPerStepQuad = 974;
 constexpr uint32_t kOpsPerObstacleTest = 6;
+constexpr uint32_t kOpsPerGridLookup = 24;  // six cell coordinates of the step box
+
+constexpr uint32_t kGridDim = 16;           // obstacle grid cells per axis
+constexpr uint32_t kGridCells = kGridDim * kGridDim * kGridDim;
+constexpr uint32_t kGridMaxVisit = 8;       // cells a step box may visit before falling back to all boxes
+constexpr uint32_t kMaxObstacles = 65535;   // grid items are 16-bit box indices
 
 // error bits in Sched::error
 constexpr uint32_t kErrLookbackTimeout = 1u;
@@ -81,6 +87,13 @@ struct QueryParams {
     unsigned long long* tiles_old;   // [tiles_per_chain] look-back words, re-activation chain
     unsigned long long* tiles_slot;  // [tiles_per_chain] look-back words, append chain
     float* path;          // [max_iterations + 2][sample_dim] goal -> root rows
+    // uniform grid over the workspace listing the boxes that touch each cell
+    // (built on the device at admission); lets a step box test only the boxes
+    // of the cells it overlaps
+    uint32_t grid_dim;     // cells per axis
+    uint32_t grid_budget;  // capacity of grid_items
+    uint32_t* grid_start;  // [grid_dim^3 + 2] CSR starts; [G^3] total, [G^3 + 1] 1 = usable
+    uint16_t* grid_items;  // [grid_budget] box indices, cell by cell
 };
 
 struct QueryState {
@@ -105,6 +118,7 @@ struct QueryState {
     unsigned long long t_start;  // %globaltimer at admission (ns)
     unsigned long long t_end;
     unsigned long long steps;    // RK4 steps executed over all samples
+    unsigned long long tests;    // step-box x box tests performed
 };
 
 struct Sched {

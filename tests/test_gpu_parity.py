@@ -202,6 +202,29 @@ def test_plan_edge_cases():
     assert_same_plan(*plan_gpu(q), O.plan(q))
 
 
+def test_plan_obstacle_grid_edge_cases():
+    """Boxes the culling grid must still find: large boxes spanning many
+    cells, inverted (min > max) boxes, boxes partly outside the workspace,
+    boxes whose faces lie exactly on grid-cell boundaries."""
+    q = W.double_integrator_query(seed=11)
+    extra = np.float32([
+        [0.30, 0.30, 0.30, 0.80, 0.55, 0.60],     # spans many cells
+        [0.70, 0.20, 0.20, 0.60, 0.10, 0.10],     # inverted
+        [-0.2, 0.40, 0.40, 0.05, 0.45, 0.45],     # outside on -x
+        [0.9375, 0.5, 0.5, 1.3, 0.5625, 0.5625],  # faces on 1/16 boundaries, outside on +x
+        [0.25, 0.25, 0.0, 0.3125, 0.3125, 0.0625],
+    ])
+    q.obstacles = np.concatenate([q.obstacles, extra]).astype(np.float32)
+    q.config = q.config.replace(tree_capacity=30_000, max_iterations=40)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+    # function level with the same boxes: verdicts equal brute force
+    cfg = q.config
+    x0, u = random_inputs(cfg, 4096, 21)
+    gx, gv, _, _ = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, _, _ = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert np.array_equal(gv, ov)
+
+
 # ---------------------------------------------------------------------------
 # batched and served forms
 # ---------------------------------------------------------------------------
