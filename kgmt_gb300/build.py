@@ -78,7 +78,27 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_cli(force=force)
     return LIB
+
+
+CLI_SRC = PKG / "cli" / "kgmt_plan.cpp"
+CLI = OUT_DIR / "kgmt_plan"
+
+
+def build_cli(force: bool = False) -> Path:
+    """The C++ command-line driver (kgmt_gb300/cli/kgmt_plan.cpp), linked
+    against libkgmt.so and the CUDA runtime."""
+    deps = [CLI_SRC, ROOT / "include" / "kgmt.hpp", ROOT / "include" / "kgmt.h", LIB]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    cuda = Path(nvcc()).resolve().parent.parent
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{ROOT / 'include'}", f"-I{cuda / 'include'}", str(CLI_SRC), "-o", str(CLI),
+           f"-L{OUT_DIR}", "-lkgmt", f"-L{cuda / 'lib64'}", "-lcudart", "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath,{cuda / 'lib64'}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 def main(argv=None) -> int:
