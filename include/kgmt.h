@@ -206,6 +206,26 @@ KGMT_API kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uint3
 /* takes up to max finished results (FIFO by completion) */
 KGMT_API kgmt_status kgmt_server_poll(kgmt_server* s, kgmt_result* out, uint32_t max, uint32_t* n_out);
 
+/* ---- single query without any allocation ----
+ * No counterpart in the reference (its planner allocates everything in its
+ * constructor).  For callers that cannot call cudaMalloc: processes whose
+ * device memory is owned by a fixed pool set up at start-up, real-time loops
+ * that must never enter the allocator, hosts that forbid allocation after
+ * initialisation.  The working memory lives in a static device array of
+ * 32 MiB that every GPU loading this library holds until exit; queries that
+ * need more (see kgmt_query_bytes) are rejected with KGMT_ERR_INVALID_ARG.
+ * The caller passes the start / goal rows (host), the obstacles (device,
+ * [n][6]) and device output buffers for up to max_nodes tree nodes
+ * (samples [max_nodes][sample_dim], parents, costs) and max_path_rows path
+ * rows (goal -> root); any output pointer may be NULL.  All calls on a device
+ * share that one array and it keeps the last call's contents: calls that
+ * overlap on the GPU (other threads, other streams) race and corrupt each
+ * other.  The first call on a device looks up the array's address; make it
+ * before any stream capture.  Blocks until done; stream may be NULL. */
+KGMT_API kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                       uint32_t n_obstacles, float* d_samples, int32_t* d_parents, float* d_costs, uint32_t max_nodes,
+                                       float* d_path, uint32_t max_path_rows, kgmt_result* result, void* stream);
+
 /* ---- function-level kernel (tests, tooling) ---- */
 /* Propagates n samples: d_x0 [n][D] parents, d_uniforms [n][8] the draws
  * (controls, steps, accept), d_obstacles [m][6].  Outputs d_x1 [n][D],

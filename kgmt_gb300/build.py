@@ -24,7 +24,7 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 BUILD_DIR = PKG / "_build"
 LIB = OUT_DIR / "libkgmt.so"
-SOURCES = ["kgmt_kernels.cu", "kgmt_engine.cu", "kgmt_abi.cu"]
+SOURCES = ["kgmt_kernels.cu", "kgmt_engine.cu", "kgmt_abi.cu", "kgmt_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

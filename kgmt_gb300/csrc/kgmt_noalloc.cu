@@ -1,0 +1,182 @@
+// kgmt_noalloc.cu -- kgmt_plan_noalloc: one planning query that allocates no
+// memory at all.
+//
+// For callers that cannot call cudaMalloc: code running under a memory
+// manager that owns every device byte (a fixed pool carved out at start-up,
+// a real-time loop that must not hit the allocator), plug-in hosts that
+// forbid allocation after initialisation.  The planner's working memory --
+// engine descriptors, tree, frontier lists, unexplored samples, region
+// tables, look-back words, path rows -- lives in the file-scope device array
+// g_noalloc_scratch below, which every GPU that loads this library holds until
+// the process exits.  The caller passes the obstacles and the output buffers.
+//
+// Rules of use:
+//  * queries whose working memory exceeds kNoAllocScratchBytes are rejected
+//    with KGMT_ERR_INVALID_ARG (kgmt_query_bytes() tells the size);
+//  * every call on a device shares the one array, and it keeps the contents
+//    of the last call: the entry point clears what must start at zero.  Calls
+//    that overlap on the GPU (two host threads, or two streams) race on the
+//    array and corrupt each other;
+//  * the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress, with that device current); make that first call
+//    before any stream capture.
+//  * no CUDA graph, event or stream is created; iterations are launched
+//    directly on the caller's stream.
+#include <cstring>
+#include <mutex>
+
+#include "kgmt_engine.h"
+
+namespace kgmt {
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;  // 32 MiB per device
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// host-side cache of the array's device address, one per device
+static unsigned char* g_scratch_addr[kNoAllocMaxDevices];
+static std::mutex g_scratch_mu;
+
+static kgmt_status scratch_address(unsigned char** out)
+{
+    int dev = 0;
+    kgmt_status st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if(st != KGMT_OK) return st;
+    if(dev < 0 || dev >= kNoAllocMaxDevices)
+        {
+            set_error("kgmt_plan_noalloc: device index out of range");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if(g_scratch_addr[dev] == nullptr)
+        {
+            void* p = nullptr;
+            st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+            if(st != KGMT_OK) return st;
+            g_scratch_addr[dev] = (unsigned char*)p;
+        }
+    *out = g_scratch_addr[dev];
+    return KGMT_OK;
+}
+
+static size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace kgmt
+
+using namespace kgmt;
+
+#define NA_CHECK(expr)                      \
+    do {                                    \
+        kgmt_status st_ = (expr);           \
+        if(st_ != KGMT_OK) return st_;      \
+    } while(0)
+
+extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                         uint32_t n_obstacles, float* d_samples, int32_t* d_parents, float* d_costs, uint32_t max_nodes,
+                                         float* d_path, uint32_t max_path_rows, kgmt_result* result, void* stream)
+{
+    if(!cfg || !h_initial || !h_goal || !result)
+        {
+            set_error("kgmt_plan_noalloc: NULL argument");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    if(n_obstacles > 0 && !d_obstacles)
+        {
+            set_error("kgmt_plan_noalloc: obstacles pointer is NULL");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    NA_CHECK(validate_config(*cfg));
+    int dev_count = 0;
+    if(cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+        {
+            cudaGetLastError();
+            set_error("no CUDA device");
+            return KGMT_ERR_NO_DEVICE;
+        }
+    // working memory: engine descriptors, then the query chunk
+    const size_t off_params = 0;
+    const size_t off_state = round256(off_params + sizeof(QueryParams));
+    const size_t off_sched = round256(off_state + sizeof(QueryState));
+    const size_t off_tiles = round256(off_sched + sizeof(Sched));
+    const size_t off_chunk = round256(off_tiles + 5 * sizeof(uint32_t));
+    const QueryLayout L = layout_of(*cfg, n_obstacles, true);
+    const size_t need = off_chunk + L.total;
+    if(need > kNoAllocScratchBytes)
+        {
+            set_error("kgmt_plan_noalloc: the query needs " + std::to_string(need) + " bytes of working memory; the static scratch holds " +
+                      std::to_string(kNoAllocScratchBytes) + " (reduce tree_capacity, or use kgmt_plan)");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    unsigned char* base = nullptr;
+    NA_CHECK(scratch_address(&base));
+    cudaStream_t s = (cudaStream_t)stream;
+
+    QueryParams* d_params = (QueryParams*)(base + off_params);
+    QueryState* d_state = (QueryState*)(base + off_state);
+    Sched* d_sched = (Sched*)(base + off_sched);
+    uint32_t* d_tiles = (uint32_t*)(base + off_tiles);
+    LaunchArgs a{d_params, d_state, d_sched, d_tiles, d_tiles + 2, d_tiles + 4};
+
+    const uint32_t block = 256;
+    int dev = 0, sms = 0;
+    NA_CHECK(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+    NA_CHECK(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
+    const int grid_a = sms * propagate_blocks_per_sm((int)block);
+    const int grid_c = sms * append_blocks_per_sm();
+
+    // the array keeps the previous call's contents: reset what starts at zero
+    const QueryParams params = make_params(*cfg, h_initial, h_goal, (char*)(base + off_chunk), L, nullptr, n_obstacles);
+    Sched sched;
+    std::memset(&sched, 0, sizeof(sched));
+    sched.n_slots = 1;
+    sched.prop_tile = block;
+    NA_CHECK(cuda_status(cudaMemcpyAsync(d_params, &params, sizeof(params), cudaMemcpyHostToDevice, s), "upload(params)"));
+    NA_CHECK(cuda_status(cudaMemcpyAsync(d_sched, &sched, sizeof(sched), cudaMemcpyHostToDevice, s), "upload(sched)"));
+    NA_CHECK(cuda_status(cudaMemsetAsync(d_state, 0xFF, sizeof(QueryState), s), "memset(state)"));
+    NA_CHECK(cuda_status(cudaMemsetAsync(d_tiles, 0, 5 * sizeof(uint32_t), s), "memset(tiles)"));
+    // params and sched live on this host stack frame: finish the copies first
+    NA_CHECK(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    NA_CHECK(cuda_status(launch_stage_obstacles(d_obstacles, params.obstacles, n_obstacles, s), "stage obstacles"));
+    NA_CHECK(cuda_status(launch_admit(a, 0, 1, s), "k_admit"));
+    NA_CHECK(cuda_status(launch_schedule(a, s), "k_schedule"));
+
+    // iterations until the query stops; poll the running count every 4
+    uint32_t running = 1;
+    for(uint32_t it = 0; it < cfg->max_iterations + 8 && running; it += 4)
+        {
+            for(int k = 0; k < 4; ++k)
+                {
+                    NA_CHECK(cuda_status(launch_propagate(a, (int)block, grid_a, s), "k_propagate"));
+                    NA_CHECK(cuda_status(launch_score(a, 1, s), "k_score"));
+                    NA_CHECK(cuda_status(launch_append(a, grid_c, s), "k_append"));
+                }
+            NA_CHECK(cuda_status(cudaMemcpyAsync(&running, &d_sched->running, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "poll"));
+            NA_CHECK(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+        }
+    NA_CHECK(cuda_status(launch_paths(a, 1, s), "k_paths"));
+    QueryState state;
+    uint32_t err = 0;
+    NA_CHECK(cuda_status(cudaMemcpyAsync(&state, d_state, sizeof(state), cudaMemcpyDeviceToHost, s), "download(state)"));
+    NA_CHECK(cuda_status(cudaMemcpyAsync(&err, &d_sched->error, sizeof(err), cudaMemcpyDeviceToHost, s), "download(error)"));
+    NA_CHECK(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    if(err != 0)
+        {
+            set_error("kgmt_plan_noalloc: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+            return KGMT_ERR_TIMEOUT;
+        }
+    // outputs into the caller's buffers
+    const uint32_t n = state.tree_size < max_nodes ? state.tree_size : max_nodes;
+    const size_t D = params.sample_dim;
+    if(d_samples && n)
+        NA_CHECK(cuda_status(cudaMemcpyAsync(d_samples, params.tree, n * D * 4, cudaMemcpyDeviceToDevice, s), "copy tree"));
+    if(d_parents && n)
+        NA_CHECK(cuda_status(cudaMemcpyAsync(d_parents, params.parent, n * 4ull, cudaMemcpyDeviceToDevice, s), "copy parents"));
+    if(d_costs && n) NA_CHECK(cuda_status(cudaMemcpyAsync(d_costs, params.cost, n * 4ull, cudaMemcpyDeviceToDevice, s), "copy costs"));
+    const uint32_t rows = state.path_len < max_path_rows ? state.path_len : max_path_rows;
+    if(d_path && rows)
+        NA_CHECK(cuda_status(cudaMemcpyAsync(d_path, params.path, (size_t)rows * D * 4, cudaMemcpyDeviceToDevice, s), "copy path"));
+    NA_CHECK(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    *result = to_result(state, 0);
+    return KGMT_OK;
+}
