@@ -173,6 +173,7 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
     p->params = make_params(p->cfg, h_initial, h_goal, p->arena.base() + off, L, nullptr, n_obstacles);
     CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, p->params.obstacles, n_obstacles, p->eng.stream()), "stage obstacles"));
     p->eng.host_params(0) = p->params;
+    p->eng.set_models(Engine::model_bit(p->cfg.model));
     CHECK_ST(p->eng.admit(0, 1, 1));
     CHECK_ST(p->eng.run_until_done(p->cfg.max_iterations));
     CHECK_ST(p->eng.extract_paths(1));
@@ -305,6 +306,9 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
     RETURN_IF(!b->arena.alloc(obs_bytes ? obs_bytes : 256, &obs_off), KGMT_ERR_OOM, "batch: arena");
     RETURN_IF(!b->arena.alloc(raw_bytes ? raw_bytes : 256, &rawo), KGMT_ERR_OOM, "batch: arena");
     float4* region = (float4*)(b->arena.base() + obs_off);
+    int models = 0;
+    for(uint32_t i = 0; i < n; ++i) models |= Engine::model_bit(cfgs[i].model);
+    b->eng.set_models(models);
     b->params.resize(n);
     for(uint32_t i = 0; i < n; ++i)
         {
@@ -430,7 +434,7 @@ extern "C" kgmt_status kgmt_batch_autotune(kgmt_batch* b, uint32_t n, const kgmt
                                            uint32_t* best_block)
 {
     RETURN_IF(!b, KGMT_ERR_INVALID_ARG, "kgmt_batch_autotune: NULL batch");
-    const uint32_t blocks[4] = {64, 128, 256, 512};
+    const uint32_t blocks[3] = {128, 256, 512};
     double best_t = 1e30;
     uint32_t best = b->eng.prop_block();
     for(uint32_t blk : blocks)
@@ -466,6 +470,7 @@ struct PendingQuery {
 
 struct ResidentQuery {
     bool used = false;
+    int model_bit = 0;
     uint64_t ticket = 0;
     size_t offset = 0;
     std::chrono::steady_clock::time_point submitted;
@@ -564,6 +569,7 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
             CHECK_ST(s->eng.init_slots(slot, 1));
             ResidentQuery& r = s->slots[slot];
             r.used = true;
+            r.model_bit = Engine::model_bit(q.cfg.model);
             r.ticket = q.ticket;
             r.offset = off;
             r.submitted = q.submitted;
@@ -571,7 +577,14 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
             admitted = true;
             ++s->running;
         }
-    if(admitted) CHECK_ST(s->eng.schedule());
+    if(admitted)
+        {
+            int models = 0;
+            for(size_t i = 0; i < s->slots.size(); ++i)
+                if(s->slots[i].used) models |= s->slots[i].model_bit;
+            s->eng.set_models(models);
+            CHECK_ST(s->eng.schedule());
+        }
     // ---- iterations for every resident query ----
     if(s->running) CHECK_ST(s->eng.run_iterations(s->opt.iters_per_step));
     // ---- retire finished queries ----

@@ -363,16 +363,16 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
 
 kgmt_status Engine::set_prop_block(uint32_t block)
 {
-    if(block != 64 && block != 128 && block != 256 && block != 512)
+    if(block != 128 && block != 256 && block != 512)
         {
-            set_error("propagate block must be 64, 128, 256 or 512");
+            set_error("propagate block must be 128, 256 or 512");
             return KGMT_ERR_INVALID_ARG;
         }
     prop_block_ = block;
     int dev = 0, sms = 0;
     KGMT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     KGMT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-    grid_a_ = sms * propagate_blocks_per_sm((int)block);
+    for(int m = 1; m <= 3; ++m) grid_a_[m] = sms * propagate_blocks_per_sm((int)block, m);
     grid_c_ = sms * append_blocks_per_sm();
     Sched s;
     std::memset(&s, 0, sizeof(s));
@@ -385,6 +385,18 @@ kgmt_status Engine::set_prop_block(uint32_t block)
             graph_ = nullptr;
         }
     return KGMT_OK;
+}
+
+void Engine::set_models(int mask)
+{
+    mask = (mask & 3) ? (mask & 3) : 3;
+    if(mask == models_) return;
+    models_ = mask;
+    if(graph_)
+        {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
 }
 
 kgmt_status Engine::upload_params(uint32_t first, uint32_t count)
@@ -466,7 +478,8 @@ kgmt_status Engine::record_event(cudaEvent_t* out)
 kgmt_status Engine::launch_iteration()
 {
     const LaunchArgs a = args();
-    for(int k = 0; k < 3; ++k)
+    // kernel kinds in the profile: 0 propagate (with the region scores), 2 append
+    for(int k = 0; k < 3; k += 2)
         {
             if(profile_)
                 {
@@ -474,8 +487,7 @@ kgmt_status Engine::launch_iteration()
                     if(st != KGMT_OK) return st;
                     prof_kind_.push_back(k);
                 }
-            if(k == 0) KGMT_CUDA(launch_propagate(a, (int)prop_block_, grid_a_, stream_), "k_propagate");
-            else if(k == 1) KGMT_CUDA(launch_score(a, (int)slots_, stream_), "k_score");
+            if(k == 0) KGMT_CUDA(launch_propagate(a, (int)prop_block_, models_, grid_a_[models_], stream_), "k_propagate");
             else KGMT_CUDA(launch_append(a, grid_c_, stream_), "k_append");
             if(profile_)
                 {
@@ -483,7 +495,7 @@ kgmt_status Engine::launch_iteration()
                     if(st != KGMT_OK) return st;
                 }
         }
-    launches_ += 3;
+    launches_ += 2;
     return KGMT_OK;
 }
 
@@ -538,7 +550,7 @@ kgmt_status Engine::launch_unit()
                     if(st != KGMT_OK) return st;
                 }
             KGMT_CUDA(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
-            launches_ += 3ull * iters_per_graph_;
+            launches_ += 2ull * iters_per_graph_;
         }
     else
         {

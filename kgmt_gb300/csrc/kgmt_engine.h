@@ -89,6 +89,10 @@ class Engine {
     kgmt_status read_error(uint32_t* err);
     kgmt_status set_prop_block(uint32_t block);
     uint32_t prop_block() const { return prop_block_; }
+    // model mix of the admitted queries (bit 0 double integrator, bit 1
+    // quadrotor): picks the propagate kernel variant; a change drops the graph
+    void set_models(int mask);
+    static int model_bit(int32_t model) { return model == KGMT_MODEL_QUADROTOR ? 2 : 1; }
     uint32_t iterations_launched() const { return iters_launched_; }
 
     // per-kernel CUDA-event timing (direct launches instead of the graph)
@@ -111,7 +115,9 @@ class Engine {
     uint32_t prop_block_ = 256;
     uint32_t iters_per_graph_ = 4;
     bool use_graph_ = true;
-    int grid_a_ = 0, grid_c_ = 0;
+    int grid_a_[4] = {0, 0, 0, 0};  // propagate grid per model mix
+    int grid_c_ = 0;
+    int models_ = 3;                // bit 0 double integrator, bit 1 quadrotor
     QueryParams* d_params_ = nullptr;
     QueryState* d_states_ = nullptr;
     Sched* d_sched_ = nullptr;

@@ -1,7 +1,7 @@
 // kgmt_kernels.cu -- the per-iteration kernel chain of the KGMT planning loop.
 //
 // One iteration of every running query (reference: KGMT::plan loop body,
-// src/planners/KGMT.cu:84-95) is three launches with fixed shapes, so the
+// src/planners/KGMT.cu:84-95) is two launches with fixed shapes, so the
 // chain can be captured once in a CUDA graph and replayed:
 //
 //   k_propagate  KGMT::propagateFrontier + propagateFrontier_kernel1/2
@@ -9,8 +9,9 @@
 //                taking propagate tiles from a ticket counter, obstacles of
 //                the tile's query staged in shared memory by a bulk (TMA)
 //                copy, warp-aggregated atomics into the region histograms.
-//   k_score      Graph::updateVertices (Graph.cu:207-358): one block per
-//                query, region scores summed in a fixed order.
+//                The block that finishes a query's last propagate tile
+//                then runs Graph::updateVertices (Graph.cu:207-358) for that
+//                query: region scores summed in a fixed order.
 //   k_append     KGMT::updateFrontier + updateFrontier_kernel
 //                (KGMT.cu:305-403) and the next iteration's frontier
 //                compaction / repeat expansion (KGMT.cu:167-181,
@@ -313,6 +314,11 @@ __global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32
             p.marks[r] = 0ull;
             p.newmarks[r] = 0ull;
         }
+    for(uint32_t i = threadIdx.x; i < p.tiles_per_chain; i += blockDim.x)
+        {
+            p.tiles_old[i] = 0ull;
+            p.tiles_slot[i] = 0ull;
+        }
     for(uint32_t j = threadIdx.x; j < p.sample_dim; j += blockDim.x) p.tree[j] = p.init[j];
     if(threadIdx.x < kRootRepeat) p.rep_new[threadIdx.x] = 0u;
     if(threadIdx.x == 0)
@@ -418,39 +424,64 @@ __global__ void k_schedule(const QueryParams* __restrict__ P, const QueryState* 
 }
 
 // ---------------------------------------------------------------------------
-// propagate
+// propagate (+ the region scores of each query, computed by the block that
+// finishes the query's last propagate tile)
 // ---------------------------------------------------------------------------
 struct PropCtx {
     uint32_t itr, spe, n_react, n_samples;
 };
 
+struct PropShared {
+    uint32_t acc;                // accepted samples of the tile
+    uint32_t steps;              // RK4 steps of the tile
+    uint32_t tests;              // box tests of the tile
+};
+
+// sample rows of a model
 template <int MODEL>
-__device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCtx& c, const float4* obs, uint32_t n_obs, uint32_t s,
-                                              bool live, QueryState* st)
+struct ModelDims {
+    static constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
+    static constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
+};
+
+// gather the parent row and draw the sample's uniforms (no obstacle access,
+// so it runs while the tile's boxes are still in flight)
+template <int MODEL>
+__device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const PropCtx& c, uint32_t s, float* x0, float* u)
 {
-    constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
-    constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
+    constexpr int D = ModelDims<MODEL>::D;
+    const uint32_t e = s / c.spe;
+    const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
+    const float* src = p.tree + (size_t)par * D;
+#pragma unroll
+    for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
+    const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
+    const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
+    const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
+    u[0] = u01(a.x), u[1] = u01(a.y), u[2] = u01(a.z), u[3] = u01(a.w);
+    u[4] = u01(b.x), u[5] = u01(b.y), u[6] = u01(b.z), u[7] = u01(b.w);
+    return par;
+}
+
+template <int MODEL>
+__device__ __forceinline__ void finish_sample(const QueryParams& p, const float4* obs, uint32_t n_obs, uint32_t s, bool live,
+                                              uint32_t par, const float* x0, const float* u, PropShared* sh)
+{
+    constexpr int D = ModelDims<MODEL>::D;
+    constexpr int NC = ModelDims<MODEL>::NC;
     const unsigned full = 0xffffffffu;
-    int r1 = -1, r2 = 0;
+    int r1 = -1;
+    uint64_t bit = 0ull;
     PropCount cnt;
     bool ok = false, acc = false;
     if(live)
         {
-            const uint32_t e = s / c.spe;
-            const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
-            float x0[D], x1[D];
-            const float* src = p.tree + (size_t)par * D;
-#pragma unroll
-            for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
-            const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-            const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
-            const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
-            const float u[8] = {u01(a.x), u01(a.y), u01(a.z), u01(a.w), u01(b.x), u01(b.y), u01(b.z), u01(b.w)};
+            float x1[D];
             if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1, cnt);
             else ok = propagate_di(p, x0, u, obs, n_obs, x1, cnt);
             const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
             r1 = cid.r1;
-            r2 = cid.r2;
+            bit = 1ull << cid.r2;
             float* dst = p.us + (size_t)s * D;
 #pragma unroll
             for(int j = 0; j < D; ++j) dst[j] = x1[j];
@@ -458,15 +489,13 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
             p.ur1[s] = r1;
             if(ok)
                 {
-                    const uint64_t bit = 1ull << r2;
                     const bool fresh = (p.marks[r1] & bit) == 0ull;
                     acc = (u[NC + 1] < p.score[r1]) || fresh;
-                    if((p.newmarks[r1] & bit) == 0ull) atomicOr((unsigned long long*)&p.newmarks[r1], (unsigned long long)bit);
                 }
             p.uflag[s] = acc ? 1 : 0;
         }
-    // warp-aggregated histogram updates (counter over all samples, valid over
-    // valid ones), then the per-query accepted count
+    // warp-aggregated histogram updates: counter over all samples, valid over
+    // the valid ones (KGMT.cu:250-253); tile totals in shared memory
     const unsigned live_mask = __ballot_sync(full, live);
     if(live)
         {
@@ -476,21 +505,82 @@ __device__ __forceinline__ void propagate_one(const QueryParams& p, const PropCt
     const unsigned ok_mask = __ballot_sync(full, ok);
     if(ok)
         {
+            // valid count and the OR of the fine-cell bits, one atomic each per region and warp
             const unsigned peers = __match_any_sync(ok_mask, r1);
-            if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.valid[r1], __popc(peers));
+            const unsigned lo = __reduce_or_sync(peers, (unsigned)bit);
+            const unsigned hi = __reduce_or_sync(peers, (unsigned)(bit >> 32));
+            if((threadIdx.x & 31) == (__ffs(peers) - 1))
+                {
+                    atomicAdd(&p.valid[r1], __popc(peers));
+                    atomicOr((unsigned long long*)&p.newmarks[r1], ((unsigned long long)hi << 32) | lo);
+                }
         }
     const unsigned acc_mask = __ballot_sync(full, acc);
     const unsigned warp_steps = __reduce_add_sync(full, (unsigned)cnt.steps);
     const unsigned warp_tests = __reduce_add_sync(full, cnt.tests);
     if((threadIdx.x & 31) == 0)
         {
-            if(acc_mask) atomicAdd(&st->n_next, __popc(acc_mask));
-            if(warp_steps) atomicAdd(&st->steps, (unsigned long long)warp_steps);
-            if(warp_tests) atomicAdd(&st->tests, (unsigned long long)warp_tests);
+            if(acc_mask) atomicAdd(&sh->acc, (unsigned)__popc(acc_mask));
+            if(warp_steps) atomicAdd(&sh->steps, warp_steps);
+            if(warp_tests) atomicAdd(&sh->tests, warp_tests);
         }
 }
 
+// Graph::updateVertices (Graph.cu:311-358) for one query, by one block: all
+// regions scored, lane l of kScoreLanes sums regions l, l+256, ... in order,
+// then a halving tree over the lanes.  Histograms and marks were updated by
+// other blocks' atomics in this kernel: read past L1.
 template <int NT>
+__device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes)
+{
+    const float F = (float)p.fine_cells;
+    for(int l = threadIdx.x; l < kScoreLanes; l += NT)
+        {
+            float acc = 0.0f;
+            for(uint32_t r = (uint32_t)l; r < p.regions; r += kScoreLanes)
+                {
+                    const uint64_t m = __ldcg(&p.marks[r]) | __ldcg(&p.newmarks[r]);
+                    p.marks[r] = m;
+                    p.newmarks[r] = 0ull;
+                    const int32_t nv = __ldcg(&p.valid[r]);
+                    float raw = 0.0f;
+                    if(nv > 0)
+                        {
+                            const int32_t n = __ldcg(&p.counter[r]);
+                            const float cov = (float)__popcll(m) / F;
+                            const float a = p.epsilon + (float)nv;
+                            const float b = a + (float)(n - nv);
+                            const float fv = (a / b) * p.cell_volume;
+                            const float f2 = fv * fv;
+                            const float f4 = f2 * f2;
+                            const float nf = (float)n;
+                            const float den = (1.0f + cov) * (1.0f + nf * nf);
+                            raw = f4 / den;
+                        }
+                    p.score[r] = raw;
+                    acc = acc + raw;
+                }
+            lanes[l] = acc;
+        }
+    __syncthreads();
+    for(int stride = kScoreLanes / 2; stride >= 1; stride >>= 1)
+        {
+            for(int l = threadIdx.x; l < stride; l += NT) lanes[l] = lanes[l] + lanes[l + stride];
+            __syncthreads();
+        }
+    const float total = lanes[0];
+    for(uint32_t r = threadIdx.x; r < p.regions; r += NT)
+        {
+            if(__ldcg(&p.valid[r]) == 0) p.score[r] = 1.0f;
+            else p.score[r] = total > 0.0f ? p.epsilon + p.score[r] / total : p.epsilon;
+        }
+    if(threadIdx.x == 0) st.score_total = total;
+}
+
+// MODELS: bit 0 double integrator present, bit 1 quadrotor present; the
+// launch picks the variant for the admitted mix, so a single-model batch
+// pays for one model's registers only
+template <int NT, int MODELS>
 __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
 {
@@ -498,8 +588,15 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
     __shared__ alignas(8) uint64_t bar;
     __shared__ QueryParams s_p;
     __shared__ PropCtx s_c;
-    __shared__ int s_tile;
-    __shared__ int s_q;
+    __shared__ PropShared s_sh;
+    __shared__ float s_lanes[kScoreLanes];
+    __shared__ int s_tile, s_q, s_last;
+    if(blockIdx.x == 0 && threadIdx.x == 0)
+        {
+            // counters of the append kernel that follows this one
+            sched->ticket_c = 0;
+            sched->finalized = 0;
+        }
     const uint32_t total = sched->tiles_a;
     const int n_slots = (int)sched->n_slots;
     if(blockIdx.x >= total) return;
@@ -508,21 +605,26 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
             mbar_init(&bar, 1);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
-    __syncthreads();
     int cur_q = -1;
     uint32_t phase = 0;
+    uint32_t t = blockIdx.x;  // first tile static, then tickets
     for(;;)
         {
-            if(threadIdx.x == 0) s_tile = (int)atomicAdd(&sched->ticket_a, 1u);
+            if(threadIdx.x == 0)
+                {
+                    s_tile = (int)t;
+                    s_q = t < total ? find_slot(tile_base, n_slots, t) : -1;
+                    s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0;
+                    s_last = 0;
+                }
             __syncthreads();
-            const uint32_t t = (uint32_t)s_tile;
+            t = (uint32_t)s_tile;
             if(t >= total) break;
-            if(threadIdx.x == 0) s_q = find_slot(tile_base, n_slots, t);
-            __syncthreads();
             const int q = s_q;
+            bool wait_obs = false;
             if(q != cur_q)
                 {
-                    // stage the query's parameters and obstacles
+                    // stage the query's parameters; its boxes go by bulk copy
                     const uint32_t* src = (const uint32_t*)&P[q];
                     uint32_t* dst = (uint32_t*)&s_p;
                     for(int i = threadIdx.x; i < (int)(sizeof(QueryParams) / 4); i += NT) dst[i] = src[i];
@@ -543,106 +645,67 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
                                 }
                         }
                     __syncthreads();
-                    if(s_p.n_obstacles > 0 && s_p.n_obstacles <= (uint32_t)kSmemObstacles)
-                        {
-                            uint32_t spins = 0;
-                            while(!mbar_try_wait(&bar, phase))
-                                if(++spins > kSpinLimit)
-                                    {
-                                        if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
-                                        break;
-                                    }
-                            phase ^= 1u;
-                        }
+                    wait_obs = s_p.n_obstacles > 0 && s_p.n_obstacles <= (uint32_t)kSmemObstacles;
                     cur_q = q;
                 }
             const uint32_t lt = t - tile_base[q];
             const uint32_t s = lt * NT + threadIdx.x;
             const bool live = s < s_c.n_samples;
             const float4* obs = s_p.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : s_p.obstacles;
-            if(s_p.model == KGMT_MODEL_QUADROTOR) propagate_one<KGMT_MODEL_QUADROTOR>(s_p, s_c, obs, s_p.n_obstacles, s, live, &S[q]);
-            else propagate_one<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, obs, s_p.n_obstacles, s, live, &S[q]);
-            __syncthreads();
-        }
-}
-
-// ---------------------------------------------------------------------------
-// score: Graph::updateVertices with all regions scored and a fixed summation
-// order (lane l of kScoreLanes sums regions l, l+256, ... then a halving tree)
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kScoreLanes) k_score(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
-                                                       const uint32_t* __restrict__ tile_c_base,
-                                                       const uint32_t* __restrict__ tile_c_old)
-{
-    __shared__ float lanes[kScoreLanes];
-    const int q = blockIdx.x;
-    if(q == 0 && threadIdx.x == 0)
-        {
-            sched->ticket_c = 0;
-            sched->finalized = 0;
-        }
-    if(q >= (int)sched->n_slots) return;
-    QueryState& st = S[q];
-    if(st.status != KGMT_QUERY_RUNNING) return;
-    const QueryParams& p = P[q];
-    const float F = (float)p.fine_cells;
-    float acc = 0.0f;
-    for(uint32_t r = threadIdx.x; r < p.regions; r += kScoreLanes)
-        {
-            const uint64_t m = p.marks[r] | p.newmarks[r];
-            p.marks[r] = m;
-            p.newmarks[r] = 0ull;
-            const int32_t nv = p.valid[r];
-            float raw = 0.0f;
-            if(nv > 0)
+            const bool quad = (MODELS & 2) && ((MODELS & 1) == 0 || s_p.model == KGMT_MODEL_QUADROTOR);
+            float x0[KGMT_MAX_SAMPLE_DIM], u[8];
+            uint32_t par = 0;
+            if(live)
                 {
-                    const int32_t n = p.counter[r];
-                    const float cov = (float)__popcll(m) / F;
-                    const float a = p.epsilon + (float)nv;
-                    const float b = a + (float)(n - nv);
-                    const float fv = (a / b) * p.cell_volume;
-                    const float f2 = fv * fv;
-                    const float f4 = f2 * f2;
-                    const float nf = (float)n;
-                    const float den = (1.0f + cov) * (1.0f + nf * nf);
-                    raw = f4 / den;
+                    if constexpr((MODELS & 2) != 0)
+                        {
+                            if(quad) par = prepare_sample<KGMT_MODEL_QUADROTOR>(s_p, s_c, s, x0, u);
+                        }
+                    if constexpr((MODELS & 1) != 0)
+                        {
+                            if(!quad) par = prepare_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, s, x0, u);
+                        }
                 }
-            p.score[r] = raw;
-            acc = acc + raw;
-        }
-    lanes[threadIdx.x] = acc;
-    __syncthreads();
-#pragma unroll
-    for(int stride = kScoreLanes / 2; stride >= 1; stride >>= 1)
-        {
-            if((int)threadIdx.x < stride) lanes[threadIdx.x] = lanes[threadIdx.x] + lanes[threadIdx.x + stride];
+            if(wait_obs)
+                {
+                    uint32_t spins = 0;
+                    while(!mbar_try_wait(&bar, phase))
+                        if(++spins > kSpinLimit)
+                            {
+                                if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
+                                break;
+                            }
+                    phase ^= 1u;
+                }
+            if constexpr((MODELS & 2) != 0)
+                {
+                    if(quad) finish_sample<KGMT_MODEL_QUADROTOR>(s_p, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
+                }
+            if constexpr((MODELS & 1) != 0)
+                {
+                    if(!quad) finish_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
+                }
             __syncthreads();
-        }
-    const float total = lanes[0];
-    for(uint32_t r = threadIdx.x; r < p.regions; r += kScoreLanes)
-        {
-            if(p.valid[r] == 0) p.score[r] = 1.0f;
-            else p.score[r] = total > 0.0f ? p.epsilon + p.score[r] / total : p.epsilon;
-        }
-    // clear this iteration's look-back words and per-iteration accumulators
-    const uint32_t n_old = tile_c_old[q];
-    const uint32_t n_slot = (tile_c_base[q + 1] - tile_c_base[q]) - n_old;
-    for(uint32_t i = threadIdx.x; i < n_old; i += kScoreLanes) p.tiles_old[i] = 0ull;
-    for(uint32_t i = threadIdx.x; i < n_slot; i += kScoreLanes) p.tiles_slot[i] = 0ull;
-    if(threadIdx.x == 0)
-        {
-            st.score_total = total;
-            // KGMT.cu:387-388
-            const float ta = 1.0f - (float)(st.tree_size + st.n_next) / (float)p.capacity;
-            const float ie = (float)st.itr * p.epsilon;
-            const double t = (double)ta;
-            const double t5 = ((t * t) * (t * t)) * t;
-            st.f_accept = (float)((double)ie * t5);
-            st.tiles_done = 0;
-            st.react_total = 0;
-            st.acc_total = 0;
-            st.w_total = 0;
-            st.goal_cand = INT_MAX;
+            if(threadIdx.x == 0)
+                {
+                    QueryState& st = S[q];
+                    if(s_sh.acc) atomicAdd(&st.n_next, s_sh.acc);
+                    if(s_sh.steps) atomicAdd(&st.steps, (unsigned long long)s_sh.steps);
+                    if(s_sh.tests) atomicAdd(&st.tests, (unsigned long long)s_sh.tests);
+                    __threadfence();
+                    const uint32_t n_tiles = tile_base[q + 1] - tile_base[q];
+                    if(atomicAdd(&st.prop_done, 1u) == n_tiles - 1) s_last = 1;
+                    t = gridDim.x + atomicAdd(&sched->ticket_a, 1u);
+                    s_tile = (int)t;
+                }
+            __syncthreads();
+            if(s_last)
+                {
+                    __threadfence();
+                    update_scores<NT>(s_p, S[q], s_lanes);
+                }
+            t = (uint32_t)s_tile;
+            __syncthreads();
         }
 }
 
@@ -665,35 +728,57 @@ __device__ void finalize_query(const QueryParams& p, QueryState& st, Sched* sche
         }
     else if(st.itr >= p.max_iterations) st.status = KGMT_QUERY_ITER_LIMIT;
     else if(st.tree_size >= p.capacity) st.status = KGMT_QUERY_CAPACITY;
+    const uint32_t react_total = __ldcg(&st.react_total), w_total = __ldcg(&st.w_total);
+    // per-iteration accumulators start from zero next iteration
+    st.tiles_done = 0;
+    st.prop_done = 0;
+    st.react_total = 0;
+    st.acc_total = 0;
+    st.w_total = 0;
+    st.goal_cand = INT_MAX;
     if(st.status != KGMT_QUERY_RUNNING)
         {
             st.t_end = globaltimer();
             return;
         }
-    st.n_react = __ldcg(&st.react_total);
-    st.w_new = __ldcg(&st.w_total);
+    st.n_react = react_total;
+    st.w_new = w_total;
     st.itr += 1;
     st.n_next = 0;
     plan_samples(p, st);
+}
+
+// KGMT.cu:387-388
+__device__ __forceinline__ float f_accept_of(const QueryParams& p, const QueryState& st)
+{
+    const float ta = 1.0f - (float)(st.tree_size + st.n_next) / (float)p.capacity;
+    const float ie = (float)st.itr * p.epsilon;
+    const double t = (double)ta;
+    const double t5 = ((t * t) * (t * t)) * t;
+    return (float)((double)ie * t5);
 }
 
 __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                            uint32_t* tile_a_base, uint32_t* tile_c_base, uint32_t* tile_c_old)
 {
     __shared__ uint32_t scratch[34];
-    __shared__ int s_tile, s_q, s_glob;
+    __shared__ int s_tile, s_q, s_glob, s_fin;
     __shared__ unsigned long long s_prefix;
+    __shared__ float s_fa;
     const uint32_t total = sched->tiles_c;
     const int n_slots = (int)sched->n_slots;
     if(blockIdx.x >= total) return;
+    uint32_t next = blockIdx.x;  // first tile static, then tickets
     for(;;)
         {
             if(threadIdx.x == 0)
                 {
-                    const uint32_t t = atomicAdd(&sched->ticket_c, 1u);
+                    const uint32_t t = next;
                     s_tile = (int)t;
                     s_q = t < total ? find_slot(tile_c_base, n_slots, t) : -1;
                     s_glob = 0;
+                    s_fin = 0;
+                    if(t < total) s_fa = f_accept_of(P[s_q], S[s_q]);
                 }
             __syncthreads();
             const uint32_t t = (uint32_t)s_tile;
@@ -709,7 +794,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                 {
                     // ---- re-activation of old nodes (KGMT.cu:364-377) ----
                     const uint32_t i0 = lt * kTileC + threadIdx.x * 4;
-                    const float fa = st.f_accept;
+                    const float fa = s_fa;
                     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
                     uint32_t flags = 0, cnt = 0;
 #pragma unroll
@@ -800,13 +885,29 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     if(done == n_tiles - 1)
                         {
                             __threadfence();
+                            if(threadIdx.x == 0) st.f_accept = s_fa;
                             finalize_query(p, st, sched);
+                            s_fin = 1;
+                        }
+                    next = gridDim.x + atomicAdd(&sched->ticket_c, 1u);
+                }
+            __syncthreads();
+            if(s_fin)
+                {
+                    // every tile of this query is done: clear its look-back
+                    // words for the next iteration, then count it finalised
+                    const uint32_t n_tiles = tile_c_base[q + 1] - tile_c_base[q];
+                    for(uint32_t i = threadIdx.x; i < n_old; i += kAppendThreads) p.tiles_old[i] = 0ull;
+                    for(uint32_t i = threadIdx.x; i < n_tiles - n_old; i += kAppendThreads) p.tiles_slot[i] = 0ull;
+                    __syncthreads();
+                    if(threadIdx.x == 0)
+                        {
                             __threadfence();
                             const uint32_t f = atomicAdd(&sched->finalized, 1u);
                             if(f == sched->running - 1) s_glob = 1;
                         }
+                    __syncthreads();
                 }
-            __syncthreads();
             if(s_glob)
                 {
                     __threadfence();
@@ -887,34 +988,56 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
 // ---------------------------------------------------------------------------
 // host-side launch wrappers
 // ---------------------------------------------------------------------------
-template <int NT>
+template <int NT, int MODELS>
 static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, cudaStream_t s)
 {
-    k_propagate<NT><<<grid, NT, kSmemObstacles * 2 * sizeof(float4), s>>>(a.params, a.states, a.sched, a.tile_a_base);
+    k_propagate<NT, MODELS><<<grid, NT, kSmemObstacles * 2 * sizeof(float4), s>>>(a.params, a.states, a.sched, a.tile_a_base);
     return cudaGetLastError();
 }
 
-cudaError_t launch_propagate(const LaunchArgs& a, int block, int grid, cudaStream_t s)
+template <int NT>
+static cudaError_t launch_propagate_m(const LaunchArgs& a, int models, int grid, cudaStream_t s)
 {
-    switch(block)
+    switch(models)
         {
-            case 64: return launch_propagate_t<64>(a, grid, s);
-            case 128: return launch_propagate_t<128>(a, grid, s);
-            case 512: return launch_propagate_t<512>(a, grid, s);
-            default: return launch_propagate_t<256>(a, grid, s);
+            case 1: return launch_propagate_t<NT, 1>(a, grid, s);
+            case 2: return launch_propagate_t<NT, 2>(a, grid, s);
+            default: return launch_propagate_t<NT, 3>(a, grid, s);
         }
 }
 
-int propagate_blocks_per_sm(int block)
+cudaError_t launch_propagate(const LaunchArgs& a, int block, int models, int grid, cudaStream_t s)
+{
+    switch(block)
+        {
+            case 128: return launch_propagate_m<128>(a, models, grid, s);
+            case 512: return launch_propagate_m<512>(a, models, grid, s);
+            default: return launch_propagate_m<256>(a, models, grid, s);
+        }
+}
+
+template <int NT>
+static int occupancy_m(int models)
 {
     int n = 0;
     const size_t smem = kSmemObstacles * 2 * sizeof(float4);
+    switch(models)
+        {
+            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 1>, NT, smem); break;
+            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 2>, NT, smem); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 3>, NT, smem); break;
+        }
+    return n;
+}
+
+int propagate_blocks_per_sm(int block, int models)
+{
+    int n = 0;
     switch(block)
         {
-            case 64: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<64>, 64, smem); break;
-            case 128: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<128>, 128, smem); break;
-            case 512: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<512>, 512, smem); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<256>, 256, smem); break;
+            case 128: n = occupancy_m<128>(models); break;
+            case 512: n = occupancy_m<512>(models); break;
+            default: n = occupancy_m<256>(models); break;
         }
     return n > 0 ? n : 1;
 }
@@ -924,12 +1047,6 @@ int append_blocks_per_sm()
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_append, kAppendThreads, 0);
     return n > 0 ? n : 1;
-}
-
-cudaError_t launch_score(const LaunchArgs& a, int n_slots, cudaStream_t s)
-{
-    k_score<<<n_slots, kScoreLanes, 0, s>>>(a.params, a.states, a.sched, a.tile_c_base, a.tile_c_old);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s)

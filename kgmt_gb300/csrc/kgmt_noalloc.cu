@@ -122,7 +122,8 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
     int dev = 0, sms = 0;
     NA_CHECK(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
     NA_CHECK(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
-    const int grid_a = sms * propagate_blocks_per_sm((int)block);
+    const int models = Engine::model_bit(cfg->model);
+    const int grid_a = sms * propagate_blocks_per_sm((int)block, models);
     const int grid_c = sms * append_blocks_per_sm();
 
     // the array keeps the previous call's contents: reset what starts at zero
@@ -147,8 +148,7 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
         {
             for(int k = 0; k < 4; ++k)
                 {
-                    NA_CHECK(cuda_status(launch_propagate(a, (int)block, grid_a, s), "k_propagate"));
-                    NA_CHECK(cuda_status(launch_score(a, 1, s), "k_score"));
+                    NA_CHECK(cuda_status(launch_propagate(a, (int)block, models, grid_a, s), "k_propagate"));
                     NA_CHECK(cuda_status(launch_append(a, grid_c, s), "k_append"));
                 }
             NA_CHECK(cuda_status(cudaMemcpyAsync(&running, &d_sched->running, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "poll"));

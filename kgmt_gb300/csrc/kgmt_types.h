@@ -108,6 +108,7 @@ struct QueryState {
     int32_t goal_cand;    // smallest new tree index in the goal ball (atomicMin)
     int32_t goal_index;
     uint32_t tiles_done;  // append/re-activation tiles finished this iteration
+    uint32_t prop_done;   // propagate tiles finished this iteration
     uint32_t react_total; // atomics of the append kernel
     uint32_t acc_total;
     uint32_t w_total;
