@@ -91,6 +91,24 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned 
     *(volatile unsigned long long*)p = v;
 }
 
+// Tile bases of up to kBaseCache slots are copied to shared memory once per
+// block, so finding a tile's query is a binary search in shared memory
+// instead of ~log2(slots) dependent global loads.
+constexpr int kBaseCache = 2048;
+
+struct BaseCache {
+    const uint32_t* base;  // shared copy, or the global array when too many slots
+    int n;
+};
+
+__device__ __forceinline__ BaseCache cache_bases(const uint32_t* __restrict__ g, int n, uint32_t* s)
+{
+    if(n + 1 > kBaseCache) return {g, n};
+    for(int i = threadIdx.x; i <= n; i += blockDim.x) s[i] = g[i];
+    __syncthreads();
+    return {s, n};
+}
+
 // last slot q with base[q] <= t (base is an exclusive prefix over n slots,
 // base[n] = total, t < total)
 __device__ __forceinline__ int find_slot(const uint32_t* __restrict__ base, int n, uint32_t t)
@@ -431,6 +449,8 @@ struct PropCtx {
     uint32_t itr, spe, n_react, n_samples;
 };
 
+constexpr int kSortBins = 32;  // step-count bins of the in-tile sort (last bin: dead lanes)
+
 struct PropShared {
     uint32_t acc;                // accepted samples of the tile
     uint32_t steps;              // RK4 steps of the tile
@@ -443,6 +463,24 @@ struct ModelDims {
     static constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
     static constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
 };
+
+// RK4 steps sample s will take (its step uniform alone), for ordering the
+// samples of a tile so that a warp's lanes loop about equally long
+template <int MODEL>
+__device__ __forceinline__ int sample_steps(const QueryParams& p, const PropCtx& c, uint32_t s)
+{
+    const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
+    if constexpr(MODEL == KGMT_MODEL_QUADROTOR)
+        {
+            const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
+            return draw_steps(p, u01(b.x));
+        }
+    else
+        {
+            const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
+            return draw_steps(p, u01(a.w));
+        }
+}
 
 // gather the parent row and draw the sample's uniforms (no obstacle access,
 // so it runs while the tile's boxes are still in flight)
@@ -543,7 +581,8 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
                     p.marks[r] = m;
                     p.newmarks[r] = 0ull;
                     const int32_t nv = __ldcg(&p.valid[r]);
-                    float raw = 0.0f;
+                    float raw = 0.0f;  // adds nothing to the total
+                    float keep = -1.0f;  // marks "no valid sample" for the normalisation pass
                     if(nv > 0)
                         {
                             const int32_t n = __ldcg(&p.counter[r]);
@@ -556,8 +595,9 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
                             const float nf = (float)n;
                             const float den = (1.0f + cov) * (1.0f + nf * nf);
                             raw = f4 / den;
+                            keep = raw;
                         }
-                    p.score[r] = raw;
+                    p.score[r] = keep;
                     acc = acc + raw;
                 }
             lanes[l] = acc;
@@ -569,11 +609,14 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
             __syncthreads();
         }
     const float total = lanes[0];
-    for(uint32_t r = threadIdx.x; r < p.regions; r += NT)
-        {
-            if(__ldcg(&p.valid[r]) == 0) p.score[r] = 1.0f;
-            else p.score[r] = total > 0.0f ? p.epsilon + p.score[r] / total : p.epsilon;
-        }
+    // each lane re-reads only what it wrote itself (raw score, -1 for regions
+    // without valid samples)
+    for(int l = threadIdx.x; l < kScoreLanes; l += NT)
+        for(uint32_t r = (uint32_t)l; r < p.regions; r += kScoreLanes)
+            {
+                const float raw = p.score[r];
+                p.score[r] = raw < 0.0f ? 1.0f : (total > 0.0f ? p.epsilon + raw / total : p.epsilon);
+            }
     if(threadIdx.x == 0) st.score_total = total;
 }
 
@@ -581,7 +624,7 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
 // launch picks the variant for the admitted mix, so a single-model batch
 // pays for one model's registers only
 template <int NT, int MODELS>
-__global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+__global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
 {
     extern __shared__ float4 s_obs[];  // kSmemObstacles * 2
@@ -590,6 +633,9 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
     __shared__ PropCtx s_c;
     __shared__ PropShared s_sh;
     __shared__ float s_lanes[kScoreLanes];
+    __shared__ uint32_t s_base[kBaseCache];
+    __shared__ uint32_t s_hist[kSortBins];
+    __shared__ uint32_t s_perm[NT];
     __shared__ int s_tile, s_q, s_last;
     if(blockIdx.x == 0 && threadIdx.x == 0)
         {
@@ -605,6 +651,7 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
             mbar_init(&bar, 1);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
+    const BaseCache bases = cache_bases(tile_base, n_slots, s_base);
     int cur_q = -1;
     uint32_t phase = 0;
     uint32_t t = blockIdx.x;  // first tile static, then tickets
@@ -613,7 +660,7 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
             if(threadIdx.x == 0)
                 {
                     s_tile = (int)t;
-                    s_q = t < total ? find_slot(tile_base, n_slots, t) : -1;
+                    s_q = t < total ? find_slot(bases.base, bases.n, t) : -1;
                     s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0;
                     s_last = 0;
                 }
@@ -648,11 +695,50 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
                     wait_obs = s_p.n_obstacles > 0 && s_p.n_obstacles <= (uint32_t)kSmemObstacles;
                     cur_q = q;
                 }
-            const uint32_t lt = t - tile_base[q];
-            const uint32_t s = lt * NT + threadIdx.x;
+            const uint32_t lt = t - bases.base[q];
+            const bool quad = (MODELS & 2) && ((MODELS & 1) == 0 || s_p.model == KGMT_MODEL_QUADROTOR);
+            // counting sort of the tile's samples by step count (dead lanes
+            // last): thread i then takes the i-th sample in that order
+            {
+                const uint32_t s0 = lt * NT + threadIdx.x;
+                int key = kSortBins - 1;
+                if(s0 < s_c.n_samples)
+                    {
+                        int k = 1;
+                        if constexpr((MODELS & 2) != 0)
+                            {
+                                if(quad) k = sample_steps<KGMT_MODEL_QUADROTOR>(s_p, s_c, s0);
+                            }
+                        if constexpr((MODELS & 1) != 0)
+                            {
+                                if(!quad) k = sample_steps<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, s0);
+                            }
+                        key = k < kSortBins - 1 ? k : kSortBins - 2;
+                    }
+                if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = 0;
+                __syncthreads();
+                const uint32_t rank = atomicAdd(&s_hist[key], 1u);
+                __syncthreads();
+                if(threadIdx.x < 32)
+                    {
+                        // exclusive scan of the bins (kSortBins <= 32)
+                        const uint32_t v = threadIdx.x < kSortBins ? s_hist[threadIdx.x] : 0u;
+                        uint32_t x = v;
+#pragma unroll
+                        for(int o = 1; o < 32; o <<= 1)
+                            {
+                                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                                if(threadIdx.x >= (unsigned)o) x += y;
+                            }
+                        if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = x - v;
+                    }
+                __syncthreads();
+                s_perm[s_hist[key] + rank] = s0;
+                __syncthreads();
+            }
+            const uint32_t s = s_perm[threadIdx.x];
             const bool live = s < s_c.n_samples;
             const float4* obs = s_p.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : s_p.obstacles;
-            const bool quad = (MODELS & 2) && ((MODELS & 1) == 0 || s_p.model == KGMT_MODEL_QUADROTOR);
             float x0[KGMT_MAX_SAMPLE_DIM], u[8];
             uint32_t par = 0;
             if(live)
@@ -693,7 +779,7 @@ __global__ void __launch_bounds__(NT) k_propagate(const QueryParams* __restrict_
                     if(s_sh.steps) atomicAdd(&st.steps, (unsigned long long)s_sh.steps);
                     if(s_sh.tests) atomicAdd(&st.tests, (unsigned long long)s_sh.tests);
                     __threadfence();
-                    const uint32_t n_tiles = tile_base[q + 1] - tile_base[q];
+                    const uint32_t n_tiles = bases.base[q + 1] - bases.base[q];
                     if(atomicAdd(&st.prop_done, 1u) == n_tiles - 1) s_last = 1;
                     t = gridDim.x + atomicAdd(&sched->ticket_a, 1u);
                     s_tile = (int)t;
@@ -765,9 +851,15 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
     __shared__ int s_tile, s_q, s_glob, s_fin;
     __shared__ unsigned long long s_prefix;
     __shared__ float s_fa;
+    __shared__ uint32_t s_cbase[kBaseCache];
+    __shared__ uint32_t s_cold[kBaseCache];
     const uint32_t total = sched->tiles_c;
     const int n_slots = (int)sched->n_slots;
     if(blockIdx.x >= total) return;
+    // this iteration's tile bases (the schedule rewrites the global arrays only
+    // after every tile is done)
+    const BaseCache cbase = cache_bases(tile_c_base, n_slots, s_cbase);
+    const BaseCache cold = cache_bases(tile_c_old, n_slots - 1, s_cold);
     uint32_t next = blockIdx.x;  // first tile static, then tickets
     for(;;)
         {
@@ -775,7 +867,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                 {
                     const uint32_t t = next;
                     s_tile = (int)t;
-                    s_q = t < total ? find_slot(tile_c_base, n_slots, t) : -1;
+                    s_q = t < total ? find_slot(cbase.base, cbase.n, t) : -1;
                     s_glob = 0;
                     s_fin = 0;
                     if(t < total) s_fa = f_accept_of(P[s_q], S[s_q]);
@@ -786,8 +878,8 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             const int q = s_q;
             const QueryParams& p = P[q];
             QueryState& st = S[q];
-            const uint32_t lt = t - tile_c_base[q];
-            const uint32_t n_old = tile_c_old[q];
+            const uint32_t lt = t - cbase.base[q];
+            const uint32_t n_old = cold.base[q];
             const uint32_t itr = st.itr;
             const uint32_t tree_size = st.tree_size;
             if(lt < n_old)
@@ -880,7 +972,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             if(threadIdx.x == 0)
                 {
                     __threadfence();
-                    const uint32_t n_tiles = tile_c_base[q + 1] - tile_c_base[q];
+                    const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
                     const uint32_t done = atomicAdd(&st.tiles_done, 1u);
                     if(done == n_tiles - 1)
                         {
@@ -896,7 +988,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                 {
                     // every tile of this query is done: clear its look-back
                     // words for the next iteration, then count it finalised
-                    const uint32_t n_tiles = tile_c_base[q + 1] - tile_c_base[q];
+                    const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
                     for(uint32_t i = threadIdx.x; i < n_old; i += kAppendThreads) p.tiles_old[i] = 0ull;
                     for(uint32_t i = threadIdx.x; i < n_tiles - n_old; i += kAppendThreads) p.tiles_slot[i] = 0ull;
                     __syncthreads();
