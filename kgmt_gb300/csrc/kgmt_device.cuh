@@ -152,16 +152,29 @@ __device__ __forceinline__ int grid_cell(const QueryParams& P, float x)
     return cell_index(((float)P.grid_dim * (x - P.ws_min)) / P.ws_range, (int)P.grid_dim);
 }
 
+// Where the culling grid of the current query lives: its starts (and the
+// first kSmemGridItems items) staged in shared memory by the propagate
+// kernel, the rest of the items in global memory.  start == nullptr: no grid.
+struct GridView {
+    const uint16_t* start;
+    const uint16_t* items_s;
+    const uint16_t* items_g;
+};
+
+__device__ __forceinline__ uint32_t grid_item(const GridView& g, uint32_t j)
+{
+    return j < kSmemGridItems ? g.items_s[j] : __ldg(g.items_g + j);
+}
+
 // true when the step box [a, b] (per-axis min/max) hits no obstacle
-__device__ __forceinline__ bool step_free(const QueryParams& P, const float4* __restrict__ obs, uint32_t n_obs, float ax, float ay,
-                                          float az, float bx, float by, float bz, PropCount& cnt)
+__device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& grid, const float4* __restrict__ obs, uint32_t n_obs,
+                                          float ax, float ay, float az, float bx, float by, float bz, PropCount& cnt)
 {
     if(n_obs == 0) return true;
     const float lx = ax > bx ? bx : ax, hx = ax > bx ? ax : bx;
     const float ly = ay > by ? by : ay, hy = ay > by ? ay : by;
     const float lz = az > bz ? bz : az, hz = az > bz ? az : bz;
-    const uint32_t* __restrict__ gs = P.grid_start;
-    if(gs != nullptr && __ldg(gs + kGridCells + 1) == 1u)
+    if(grid.start != nullptr)
         {
             const int x0 = grid_cell(P, lx), x1 = grid_cell(P, hx);
             const int y0 = grid_cell(P, ly), y1 = grid_cell(P, hy);
@@ -174,11 +187,11 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const float4* __
                             for(int cz = z0; cz <= z1; ++cz)
                                 {
                                     const int c = (cx * G + cy) * G + cz;
-                                    const uint32_t e = __ldg(gs + c + 1);
-                                    for(uint32_t j = __ldg(gs + c); j < e; ++j)
+                                    const uint32_t e = grid.start[c + 1];
+                                    for(uint32_t j = grid.start[c]; j < e; ++j)
                                         {
                                             ++cnt.tests;
-                                            if(box_hit(obs, __ldg(P.grid_items + j), lx, ly, lz, hx, hy, hz)) return false;
+                                            if(box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
                                         }
                                 }
                     return true;
@@ -204,7 +217,7 @@ __device__ __forceinline__ int draw_steps(const QueryParams& P, float u)
 // reference's own formula (statePropagator.cu:97-99, (5v + 2ah) h / 6).
 // x0/x1 are sample rows [x y z vx vy vz ax ay az duration].
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
+__device__ __forceinline__ bool propagate_di(const QueryParams& P, const GridView& grid, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
                                              float* x1, PropCount& cnt)
 {
     const float a0 = P.u_min[0] + u[0] * P.u_span[0];
@@ -242,7 +255,7 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const float* 
                     ok = false;
                     break;
                 }
-            if(!step_free(P, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], cnt))
+            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], cnt))
                 {
                     ok = false;
                     break;
@@ -289,7 +302,7 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
     d[11] = ((P.jz * p) * q + (P.iiz * lmn) * r) + P.iiz * nc;
 }
 
-__device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
+__device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridView& grid, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
                                                float* x1, PropCount& cnt)
 {
     const float zc = P.u_min[0] + u[0] * P.u_span[0];
@@ -329,7 +342,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const float
                     ok = false;
                     break;
                 }
-            if(!step_free(P, obs, n_obs, q0, q1, q2, s[0], s[1], s[2], cnt))
+            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, s[0], s[1], s[2], cnt))
                 {
                     ok = false;
                     break;

@@ -150,7 +150,7 @@ static size_t aligned(size_t& cur, size_t bytes)
 QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_obstacles)
 {
     QueryLayout L{};
-    L.grid_budget = n_obstacles ? std::max<uint32_t>(8192u, 32u * n_obstacles) : 0u;
+    L.grid_budget = n_obstacles ? std::min<uint32_t>(kMaxGridItems, std::max<uint32_t>(8192u, 32u * std::min(n_obstacles, 4096u))) : 0u;
     const size_t T = c.tree_capacity, D = sample_dim_of(c.model);
     const size_t R1 = (size_t)c.coarse_len * c.coarse_len * c.coarse_len;
     L.tiles_per_chain = (uint32_t)((T + kTileC - 1) / kTileC + 1);
@@ -173,7 +173,8 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_ob
     L.tiles_old = aligned(cur, (size_t)L.tiles_per_chain * 8);
     L.tiles_slot = aligned(cur, (size_t)L.tiles_per_chain * 8);
     L.path = aligned(cur, ((size_t)c.max_iterations + 2) * D * 4);
-    L.grid_start = aligned(cur, n_obstacles ? ((size_t)kGridCells + 2) * 4 : 0);
+    L.grid_meta = aligned(cur, n_obstacles ? 16 : 0);
+    L.grid_start = aligned(cur, n_obstacles ? ((size_t)kGridCells + 1) * 2 : 0);
     L.grid_items = aligned(cur, (size_t)L.grid_budget * 2);
     L.obstacles = aligned(cur, inline_obstacles ? (size_t)n_obstacles * 32 : 0);
     L.total = cur;
@@ -250,7 +251,8 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
             p.obstacles = obstacles;
             return p;
         }
-    p.grid_start = n_obstacles ? (uint32_t*)(chunk + L.grid_start) : nullptr;
+    p.grid_meta = n_obstacles ? (uint32_t*)(chunk + L.grid_meta) : nullptr;
+    p.grid_start = n_obstacles ? (uint16_t*)(chunk + L.grid_start) : nullptr;
     p.grid_items = (uint16_t*)(chunk + L.grid_items);
     p.tree = (float*)(chunk + L.tree);
     p.parent = (int32_t*)(chunk + L.parent);

@@ -407,15 +407,16 @@ __global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restric
         {
             const uint32_t c = threadIdx.x * PER + i;
             const uint32_t k = cnt[c];
-            p.grid_start[c] = run;
+            p.grid_start[c] = (uint16_t)run;  // meaningful only when usable (total <= 65535)
             cnt[c] = run;  // becomes the fill cursor
             run += k;
         }
-    const bool usable = !s_bad && total <= p.grid_budget;
+    const bool usable = !s_bad && total <= p.grid_budget && total <= kMaxGridItems;
     if(threadIdx.x == 0)
         {
-            p.grid_start[kGridCells] = total;
-            p.grid_start[kGridCells + 1] = usable ? 1u : 0u;
+            p.grid_start[kGridCells] = (uint16_t)total;
+            p.grid_meta[0] = total;
+            p.grid_meta[1] = usable ? 1u : 0u;
         }
     __syncthreads();
     if(!usable) return;
@@ -502,8 +503,8 @@ __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const P
 }
 
 template <int MODEL>
-__device__ __forceinline__ void finish_sample(const QueryParams& p, const float4* obs, uint32_t n_obs, uint32_t s, bool live,
-                                              uint32_t par, const float* x0, const float* u, PropShared* sh)
+__device__ __forceinline__ void finish_sample(const QueryParams& p, const GridView& grid, const float4* obs, uint32_t n_obs, uint32_t s,
+                                              bool live, uint32_t par, const float* x0, const float* u, PropShared* sh)
 {
     constexpr int D = ModelDims<MODEL>::D;
     constexpr int NC = ModelDims<MODEL>::NC;
@@ -515,8 +516,8 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const float4
     if(live)
         {
             float x1[D];
-            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, x0, u, obs, n_obs, x1, cnt);
-            else ok = propagate_di(p, x0, u, obs, n_obs, x1, cnt);
+            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, grid, x0, u, obs, n_obs, x1, cnt);
+            else ok = propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
             const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
             r1 = cid.r1;
             bit = 1ull << cid.r2;
@@ -627,7 +628,13 @@ template <int NT, int MODELS>
 __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
 {
-    extern __shared__ float4 s_obs[];  // kSmemObstacles * 2
+    // dynamic shared memory: boxes | grid starts | grid items | grid meta
+    extern __shared__ float4 s_dyn[];
+    float4* s_obs = s_dyn;
+    uint16_t* s_gstart = (uint16_t*)((char*)s_dyn + kSmemObsBytes);
+    uint16_t* s_gitems = (uint16_t*)((char*)s_dyn + kSmemObsBytes + kSmemStartBytes);
+    uint32_t* s_gmeta = (uint32_t*)((char*)s_dyn + kSmemObsBytes + kSmemStartBytes + kSmemItemBytes);
+    __shared__ uint32_t s_copy;
     __shared__ alignas(8) uint64_t bar;
     __shared__ QueryParams s_p;
     __shared__ PropCtx s_c;
@@ -655,6 +662,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
     int cur_q = -1;
     uint32_t phase = 0;
     uint32_t t = blockIdx.x;  // first tile static, then tickets
+    uint32_t t_next = 0;      // ticket taken while the current tile runs (thread 0)
     for(;;)
         {
             if(threadIdx.x == 0)
@@ -663,6 +671,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                     s_q = t < total ? find_slot(bases.base, bases.n, t) : -1;
                     s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0;
                     s_last = 0;
+                    if(t < total) t_next = gridDim.x + atomicAdd(&sched->ticket_a, 1u);
                 }
             __syncthreads();
             t = (uint32_t)s_tile;
@@ -682,17 +691,29 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                             s_c.spe = st.spe;
                             s_c.n_react = st.n_react;
                             s_c.n_samples = st.n_samples;
-                            const uint32_t n_obs = P[q].n_obstacles;
-                            if(n_obs > 0 && n_obs <= (uint32_t)kSmemObstacles)
+                            // boxes, grid meta, grid starts and the first grid
+                            // items: one mbarrier transaction of bulk copies
+                            const QueryParams& gp = P[q];
+                            const uint32_t n_obs = gp.n_obstacles;
+                            const bool obs_s = n_obs > 0 && n_obs <= (uint32_t)kSmemObstacles;
+                            const bool grid = gp.grid_meta != nullptr;
+                            const uint32_t bytes = (obs_s ? n_obs * 32u : 0u) + (grid ? 16u + kSmemStartBytes + kSmemItemBytes : 0u);
+                            s_copy = bytes;
+                            if(bytes)
                                 {
                                     fence_proxy_async_smem();
-                                    const uint32_t bytes = n_obs * 32u;
                                     mbar_expect_tx(&bar, bytes);
-                                    bulk_copy_g2s(s_obs, P[q].obstacles, bytes, &bar);
+                                    if(obs_s) bulk_copy_g2s(s_obs, gp.obstacles, n_obs * 32u, &bar);
+                                    if(grid)
+                                        {
+                                            bulk_copy_g2s(s_gmeta, gp.grid_meta, 16u, &bar);
+                                            bulk_copy_g2s(s_gstart, gp.grid_start, kSmemStartBytes, &bar);
+                                            bulk_copy_g2s(s_gitems, gp.grid_items, kSmemItemBytes, &bar);
+                                        }
                                 }
                         }
                     __syncthreads();
-                    wait_obs = s_p.n_obstacles > 0 && s_p.n_obstacles <= (uint32_t)kSmemObstacles;
+                    wait_obs = s_copy != 0;
                     cur_q = q;
                 }
             const uint32_t lt = t - bases.base[q];
@@ -763,13 +784,14 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                             }
                     phase ^= 1u;
                 }
+            const GridView grid{(s_p.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, s_p.grid_items};
             if constexpr((MODELS & 2) != 0)
                 {
-                    if(quad) finish_sample<KGMT_MODEL_QUADROTOR>(s_p, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
+                    if(quad) finish_sample<KGMT_MODEL_QUADROTOR>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
                 }
             if constexpr((MODELS & 1) != 0)
                 {
-                    if(!quad) finish_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
+                    if(!quad) finish_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
                 }
             __syncthreads();
             if(threadIdx.x == 0)
@@ -781,7 +803,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                     __threadfence();
                     const uint32_t n_tiles = bases.base[q + 1] - bases.base[q];
                     if(atomicAdd(&st.prop_done, 1u) == n_tiles - 1) s_last = 1;
-                    t = gridDim.x + atomicAdd(&sched->ticket_a, 1u);
+                    t = t_next;
                     s_tile = (int)t;
                 }
             __syncthreads();
@@ -1068,8 +1090,9 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
     for(int j = 0; j < D; ++j) a[j] = x0[(size_t)s * D + j];
     for(int j = 0; j < 8; ++j) u[j] = uni[(size_t)s * 8 + j];
     PropCount cnt;
-    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, a, u, s_obs, n_obs, b, cnt)
-                                              : propagate_di(p, a, u, s_obs, n_obs, b, cnt);
+    const GridView none{nullptr, nullptr, nullptr};
+    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, none, a, u, s_obs, n_obs, b, cnt)
+                                              : propagate_di(p, none, a, u, s_obs, n_obs, b, cnt);
     for(int j = 0; j < D; ++j) x1[(size_t)s * D + j] = b[j];
     valid[s] = ok ? 1 : 0;
     const CellIds c = cell_ids(p, b[0], b[1], b[2]);
@@ -1083,7 +1106,7 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
 template <int NT, int MODELS>
 static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, cudaStream_t s)
 {
-    k_propagate<NT, MODELS><<<grid, NT, kSmemObstacles * 2 * sizeof(float4), s>>>(a.params, a.states, a.sched, a.tile_a_base);
+    k_propagate<NT, MODELS><<<grid, NT, kPropSmemBytes, s>>>(a.params, a.states, a.sched, a.tile_a_base);
     return cudaGetLastError();
 }
 
@@ -1112,7 +1135,7 @@ template <int NT>
 static int occupancy_m(int models)
 {
     int n = 0;
-    const size_t smem = kSmemObstacles * 2 * sizeof(float4);
+    const size_t smem = kPropSmemBytes;
     switch(models)
         {
             case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 1>, NT, smem); break;

@@ -21,7 +21,7 @@ constexpr int kRootRepeat = 5;          // KGMT.cu:67
 constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
 constexpr int kRepeatDense = 1;         // KGMT.cu:338-339
 constexpr int kSparseValidLimit = 10;   // KGMT.cu:336
-constexpr int kSmemObstacles = 1024;    // boxes staged in shared memory per block
+constexpr int kSmemObstacles = 512;     // boxes staged in shared memory per block
 constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a device-side wait gives up
 
 constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-admitted slot
@@ -38,6 +38,13 @@ constexpr uint32_t kGridDim = 16;           // obstacle grid cells per axis
 constexpr uint32_t kGridCells = kGridDim * kGridDim * kGridDim;
 constexpr uint32_t kGridMaxVisit = 8;       // cells a step box may visit before falling back to all boxes
 constexpr uint32_t kMaxObstacles = 65535;   // grid items are 16-bit box indices
+constexpr uint32_t kMaxGridItems = 65535;   // grid starts are 16-bit
+constexpr uint32_t kSmemGridItems = 4096;   // grid items staged in shared memory per block
+// dynamic shared memory of k_propagate: boxes, grid starts, grid items, meta
+constexpr uint32_t kSmemObsBytes = kSmemObstacles * 32;
+constexpr uint32_t kSmemStartBytes = ((kGridCells + 1) * 2 + 15) / 16 * 16;
+constexpr uint32_t kSmemItemBytes = kSmemGridItems * 2;
+constexpr uint32_t kPropSmemBytes = kSmemObsBytes + kSmemStartBytes + kSmemItemBytes + 16;
 
 // error bits in Sched::error
 constexpr uint32_t kErrLookbackTimeout = 1u;
@@ -90,10 +97,11 @@ struct QueryParams {
     // uniform grid over the workspace listing the boxes that touch each cell
     // (built on the device at admission); lets a step box test only the boxes
     // of the cells it overlaps
-    uint32_t grid_dim;     // cells per axis
-    uint32_t grid_budget;  // capacity of grid_items
-    uint32_t* grid_start;  // [grid_dim^3 + 2] CSR starts; [G^3] total, [G^3 + 1] 1 = usable
-    uint16_t* grid_items;  // [grid_budget] box indices, cell by cell
+    uint32_t grid_dim;       // cells per axis
+    uint32_t grid_budget;    // capacity of grid_items (<= 65535)
+    uint32_t* grid_meta;     // [4]: [0] items in use, [1] 1 = usable
+    uint16_t* grid_start;    // [grid_dim^3 + 1] CSR starts (16-bit: at most 65535 items)
+    uint16_t* grid_items;    // [grid_budget] box indices, cell by cell
 };
 
 struct QueryState {
