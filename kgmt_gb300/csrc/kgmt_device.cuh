@@ -59,13 +59,24 @@ __device__ __forceinline__ float u01(uint32_t x) { return (float)((x >> 8) + 1u)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
 {
+    // explicit fused multiply-adds (one rounding each), placed exactly as in
+    // the CPU restatement; nothing else is contracted (-fmad=false)
     float n = rintf(x * 0x1.45f306p-1f);
-    float r = ((x - n * 0x1.92p+0f) - n * 0x1.fb4p-12f) - n * 0x1.4442d2p-24f;
+    float r = fmaf(-n, 0x1.92p+0f, x);
+    r = fmaf(-n, 0x1.fb4p-12f, r);
+    r = fmaf(-n, 0x1.4442d2p-24f, r);
     float qf = n - 4.0f * floorf(n * 0.25f);
     int q = (qf >= 0.0f && qf <= 3.0f) ? (int)qf : 0;
     float r2 = r * r;
-    float sp = r + (r * r2) * (-0x1.555556p-3f + r2 * (0x1.111112p-7f + r2 * (-0x1.a01a02p-13f + r2 * 0x1.71de3ap-19f)));
-    float cp = 1.0f + r2 * (-0x1.0p-1f + r2 * (0x1.555556p-5f + r2 * (-0x1.6c16c2p-10f + r2 * (0x1.a01a02p-16f + r2 * -0x1.27e4fcp-22f))));
+    float ps = fmaf(r2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+    ps = fmaf(r2, ps, 0x1.111112p-7f);
+    ps = fmaf(r2, ps, -0x1.555556p-3f);
+    float sp = fmaf(r * r2, ps, r);
+    float pc = fmaf(r2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+    pc = fmaf(r2, pc, -0x1.6c16c2p-10f);
+    pc = fmaf(r2, pc, 0x1.555556p-5f);
+    pc = fmaf(r2, pc, -0x1.0p-1f);
+    float cp = fmaf(r2, pc, 1.0f);
     float ss = (q & 1) ? cp : sp;
     float cc = (q & 1) ? sp : cp;
     s = (q == 2 || q == 3) ? -ss : ss;
@@ -284,22 +295,24 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
     sincos_portable(theta, sth, cth);
     sincos_portable(psi, spsi, cpsi);
     const float tth = sth / cth;
-    d[0] = ((cth * cpsi) * uu + ((sphi * sth) * cpsi - cphi * spsi) * vv) + ((cphi * sth) * cpsi + sphi * spsi) * ww;
-    d[1] = ((cth * spsi) * uu + ((sphi * sth) * spsi + cphi * cpsi) * vv) + ((cphi * sth) * spsi - sphi * cpsi) * ww;
-    d[2] = ((-sth) * uu + (sphi * cth) * vv) + (cphi * cth) * ww;
-    const float qr = q * sphi + r * cphi;
-    d[3] = p + qr * tth;
-    d[4] = q * cphi - r * sphi;
+    const float g = P.gravity;
+    const float sps = sphi * sth, cps = cphi * sth;
+    d[0] = fmaf(fmaf(cps, cpsi, sphi * spsi), ww, fmaf(fmaf(sps, cpsi, -(cphi * spsi)), vv, (cth * cpsi) * uu));
+    d[1] = fmaf(fmaf(cps, spsi, -(sphi * cpsi)), ww, fmaf(fmaf(sps, spsi, cphi * cpsi), vv, (cth * spsi) * uu));
+    d[2] = fmaf(cphi * cth, ww, fmaf(sphi * cth, vv, (-sth) * uu));
+    const float qr = fmaf(q, sphi, r * cphi);
+    d[3] = fmaf(qr, tth, p);
+    d[4] = fmaf(q, cphi, -(r * sphi));
     d[5] = qr / cth;
-    const float xyz = (-P.nu) * sqrtf((uu * uu + vv * vv) + ww * ww);
+    const float xyz = (-P.nu) * sqrtf(fmaf(ww, ww, fmaf(vv, vv, uu * uu)));
     const float mx = P.mass_inv * xyz;
-    d[6] = ((r * vv - q * ww) - P.gravity * sth) + mx * uu;
-    d[7] = ((p * ww - r * uu) + (P.gravity * cth) * sphi) + mx * vv;
-    d[8] = (((q * uu - p * vv) + (P.gravity * cth) * cphi) + mx * ww) + P.mass_inv * zc;
-    const float lmn = (-P.mu) * sqrtf((p * p + q * q) + r * r);
-    d[9] = ((P.jx * q) * r + (P.iix * lmn) * p) + P.iix * lc;
-    d[10] = ((P.jy * p) * r + (P.iiy * lmn) * q) + P.iiy * mc;
-    d[11] = ((P.jz * p) * q + (P.iiz * lmn) * r) + P.iiz * nc;
+    d[6] = fmaf(mx, uu, fmaf(-g, sth, fmaf(r, vv, -(q * ww))));
+    d[7] = fmaf(mx, vv, fmaf(g * cth, sphi, fmaf(p, ww, -(r * uu))));
+    d[8] = fmaf(P.mass_inv, zc, fmaf(mx, ww, fmaf(g * cth, cphi, fmaf(q, uu, -(p * vv)))));
+    const float lmn = (-P.mu) * sqrtf(fmaf(r, r, fmaf(q, q, p * p)));
+    d[9] = fmaf(P.iix, lc, fmaf(P.iix * lmn, p, (P.jx * q) * r));
+    d[10] = fmaf(P.iiy, mc, fmaf(P.iiy * lmn, q, (P.jy * p) * r));
+    d[11] = fmaf(P.iiz, nc, fmaf(P.iiz * lmn, r, (P.jz * p) * q));
 }
 
 __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridView& grid, const float* x0, const float* u, const float4* obs, uint32_t n_obs,
@@ -322,16 +335,16 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridV
             const float q0 = s[0], q1 = s[1], q2 = s[2];
             quad_ode(P, s, zc, lc, mc, nc, k1);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k1[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k1[j], s[j]);
             quad_ode(P, t, zc, lc, mc, nc, k2);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k2[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k2[j], s[j]);
             quad_ode(P, t, zc, lc, mc, nc, k3);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + h * k3[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(h, k3[j], s[j]);
             quad_ode(P, t, zc, lc, mc, nc, k4);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) s[j] = s[j] + h6 * (((k1[j] + 2.0f * k2[j]) + 2.0f * k3[j]) + k4[j]);
+            for(int j = 0; j < 12; ++j) s[j] = fmaf(h6, fmaf(2.0f, k3[j], fmaf(2.0f, k2[j], k1[j])) + k4[j], s[j]);
             if(s[6] < P.v_min || s[6] > P.v_max || s[7] < P.v_min || s[7] > P.v_max || s[8] < P.v_min || s[8] > P.v_max)
                 {
                     ok = false;

@@ -26,11 +26,12 @@ constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a device-side wait gi
 
 constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-admitted slot
 
-// static FP32 operation counts per RK4 step, from the code in kgmt_device.cuh
-// (multiplies, adds, divides, compares; the quadrotor's portable sine/cosine
-// counted as the float operations they are made of)
+// static FP32 lane-operation counts per RK4 step, from the code in
+// kgmt_device.cuh (a multiply, add, fused multiply-add, divide or compare is
+// one; the quadrotor's portable sine/cosine counted as the operations it is
+// made of: 4 ode evaluations of ~139, stage and update combinations, checks)
 constexpr uint32_t kOpsPerStepDI = 81;
-constexpr uint32_t kOpsPerStepQuad = 974;
+constexpr uint32_t kOpsPerStepQuad = 658;
 constexpr uint32_t kOpsPerObstacleTest = 6;
 constexpr uint32_t kOpsPerGridLookup = 24;  // six cell coordinates of the step box
 

@@ -118,13 +118,24 @@ float ko_react_uniform(uint64_t seed, uint32_t node, uint32_t itr)
 
 void ko_sincosf(float x, float* s_out, float* c_out)
 {
+    /* fused multiply-adds (fmaf, one rounding each) in the same places as the
+     * CUDA kernels */
     float n = rintf(x * KO_TWO_OVER_PI);
-    float r = ((x - n * KO_PIO2_1) - n * KO_PIO2_2) - n * KO_PIO2_3;
+    float r = fmaf(-n, KO_PIO2_1, x);
+    r = fmaf(-n, KO_PIO2_2, r);
+    r = fmaf(-n, KO_PIO2_3, r);
     float qf = n - 4.0f * floorf(n * 0.25f);
     int q = (qf >= 0.0f && qf <= 3.0f) ? (int)qf : 0;
     float r2 = r * r;
-    float sp = r + (r * r2) * (KO_S1 + r2 * (KO_S2 + r2 * (KO_S3 + r2 * KO_S4)));
-    float cp = 1.0f + r2 * (KO_C1 + r2 * (KO_C2 + r2 * (KO_C3 + r2 * (KO_C4 + r2 * KO_C5))));
+    float ps = fmaf(r2, KO_S4, KO_S3);
+    ps = fmaf(r2, ps, KO_S2);
+    ps = fmaf(r2, ps, KO_S1);
+    float sp = fmaf(r * r2, ps, r);
+    float pc = fmaf(r2, KO_C5, KO_C4);
+    pc = fmaf(r2, pc, KO_C3);
+    pc = fmaf(r2, pc, KO_C2);
+    pc = fmaf(r2, pc, KO_C1);
+    float cp = fmaf(r2, pc, 1.0f);
     float s, c;
     switch(q)
         {
@@ -412,23 +423,26 @@ static void quad_ode_f(const ko_config* c, const float* s, const quad_ctrl_f* u,
     ko_sincosf(theta, &sth, &cth);
     ko_sincosf(psi, &spsi, &cpsi);
     float tth = sth / cth;
-    d[0] = ((cth * cpsi) * uu + ((sphi * sth) * cpsi - cphi * spsi) * vv) + ((cphi * sth) * cpsi + sphi * spsi) * ww;
-    d[1] = ((cth * spsi) * uu + ((sphi * sth) * spsi + cphi * cpsi) * vv) + ((cphi * sth) * spsi - sphi * cpsi) * ww;
-    d[2] = ((-sth) * uu + (sphi * cth) * vv) + (cphi * cth) * ww;
-    float qr = q * sphi + r * cphi;
-    d[3] = p + qr * tth;
-    d[4] = q * cphi - r * sphi;
+    const float g = c->gravity;
+    const float sps = sphi * sth, cps = cphi * sth;
+    d[0] = fmaf(fmaf(cps, cpsi, sphi * spsi), ww, fmaf(fmaf(sps, cpsi, -(cphi * spsi)), vv, (cth * cpsi) * uu));
+    d[1] = fmaf(fmaf(cps, spsi, -(sphi * cpsi)), ww, fmaf(fmaf(sps, spsi, cphi * cpsi), vv, (cth * spsi) * uu));
+    d[2] = fmaf(cphi * cth, ww, fmaf(sphi * cth, vv, (-sth) * uu));
+    float qr = fmaf(q, sphi, r * cphi);
+    d[3] = fmaf(qr, tth, p);
+    d[4] = fmaf(q, cphi, -(r * sphi));
     d[5] = qr / cth;
-    float xyz = (-c->nu) * sqrtf((uu * uu + vv * vv) + ww * ww);
+    float xyz = (-c->nu) * sqrtf(fmaf(ww, ww, fmaf(vv, vv, uu * uu)));
     float mx = c->mass_inv * xyz;
-    d[6] = ((r * vv - q * ww) - c->gravity * sth) + mx * uu;
-    d[7] = ((p * ww - r * uu) + (c->gravity * cth) * sphi) + mx * vv;
-    d[8] = (((q * uu - p * vv) + (c->gravity * cth) * cphi) + mx * ww) + c->mass_inv * u->zc;
-    float lmn = (-c->mu) * sqrtf((p * p + q * q) + r * r);
+    d[6] = fmaf(mx, uu, fmaf(-g, sth, fmaf(r, vv, -(q * ww))));
+    d[7] = fmaf(mx, vv, fmaf(g * cth, sphi, fmaf(p, ww, -(r * uu))));
+    d[8] = fmaf(c->mass_inv, u->zc, fmaf(mx, ww, fmaf(g * cth, cphi, fmaf(q, uu, -(p * vv)))));
+    float lmn = (-c->mu) * sqrtf(fmaf(r, r, fmaf(q, q, p * p)));
     float iix = 1.0f / c->ix, iiy = 1.0f / c->iy, iiz = 1.0f / c->iz;
-    d[9] = ((((c->iy - c->iz) / c->ix) * q) * r + (iix * lmn) * p) + iix * u->lc;
-    d[10] = ((((c->iz - c->ix) / c->iy) * p) * r + (iiy * lmn) * q) + iiy * u->mc;
-    d[11] = ((((c->ix - c->iy) / c->iz) * p) * q + (iiz * lmn) * r) + iiz * u->nc;
+    float jx = (c->iy - c->iz) / c->ix, jy = (c->iz - c->ix) / c->iy, jz = (c->ix - c->iy) / c->iz;
+    d[9] = fmaf(iix, u->lc, fmaf(iix * lmn, p, (jx * q) * r));
+    d[10] = fmaf(iiy, u->mc, fmaf(iiy * lmn, q, (jy * p) * r));
+    d[11] = fmaf(iiz, u->nc, fmaf(iiz * lmn, r, (jz * p) * q));
 }
 
 static int prop_quad_f(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, float* x1)
@@ -447,13 +461,13 @@ static int prop_quad_f(const ko_config* c, const float* x0, const float* u, cons
         {
             float p0[3] = {s[0], s[1], s[2]};
             quad_ode_f(c, s, &qc, k1);
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k1[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k1[j], s[j]);
             quad_ode_f(c, t, &qc, k2);
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + hh * k2[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k2[j], s[j]);
             quad_ode_f(c, t, &qc, k3);
-            for(int j = 0; j < 12; ++j) t[j] = s[j] + h * k3[j];
+            for(int j = 0; j < 12; ++j) t[j] = fmaf(h, k3[j], s[j]);
             quad_ode_f(c, t, &qc, k4);
-            for(int j = 0; j < 12; ++j) s[j] = s[j] + h6 * (((k1[j] + 2.0f * k2[j]) + 2.0f * k3[j]) + k4[j]);
+            for(int j = 0; j < 12; ++j) s[j] = fmaf(h6, fmaf(2.0f, k3[j], fmaf(2.0f, k2[j], k1[j])) + k4[j], s[j]);
             if(s[6] < c->v_min || s[6] > c->v_max || s[7] < c->v_min || s[7] > c->v_max || s[8] < c->v_min || s[8] > c->v_max)
                 {
                     ok = 0;
