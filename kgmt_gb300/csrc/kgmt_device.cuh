@@ -322,29 +322,32 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridV
     const float lc = P.u_min[1] + u[1] * P.u_span[1];
     const float mc = P.u_min[2] + u[2] * P.u_span[2];
     const float nc = P.u_min[3] + u[3] * P.u_span[3];
-    const int k = draw_steps(P, u[4]);
+    const int k_steps = draw_steps(P, u[4]);
     const float h = P.step_size, hh = P.half_step, h6 = P.sixth_step;
-    float s[12], k1[12], k2[12], k3[12], k4[12], t[12];
+    // RK4 with the stage sum accumulated as each derivative arrives:
+    // acc = k1; acc = fma(2, k2, acc); acc = fma(2, k3, acc); acc += k4 is
+    // exactly fma(2, k3, fma(2, k2, k1)) + k4, with one derivative live at a time
+    float s[12], k[12], t[12], acc[12];
 #pragma unroll
     for(int j = 0; j < 12; ++j) s[j] = x0[j];
     bool ok = true;
     int done = 0;
-    for(int i = 0; i < k; ++i)
+    for(int i = 0; i < k_steps; ++i)
         {
             ++done;
             const float q0 = s[0], q1 = s[1], q2 = s[2];
-            quad_ode(P, s, zc, lc, mc, nc, k1);
+            quad_ode(P, s, zc, lc, mc, nc, k);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k1[j], s[j]);
-            quad_ode(P, t, zc, lc, mc, nc, k2);
+            for(int j = 0; j < 12; ++j) acc[j] = k[j], t[j] = fmaf(hh, k[j], s[j]);
+            quad_ode(P, t, zc, lc, mc, nc, k);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = fmaf(hh, k2[j], s[j]);
-            quad_ode(P, t, zc, lc, mc, nc, k3);
+            for(int j = 0; j < 12; ++j) acc[j] = fmaf(2.0f, k[j], acc[j]), t[j] = fmaf(hh, k[j], s[j]);
+            quad_ode(P, t, zc, lc, mc, nc, k);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) t[j] = fmaf(h, k3[j], s[j]);
-            quad_ode(P, t, zc, lc, mc, nc, k4);
+            for(int j = 0; j < 12; ++j) acc[j] = fmaf(2.0f, k[j], acc[j]), t[j] = fmaf(h, k[j], s[j]);
+            quad_ode(P, t, zc, lc, mc, nc, k);
 #pragma unroll
-            for(int j = 0; j < 12; ++j) s[j] = fmaf(h6, fmaf(2.0f, k3[j], fmaf(2.0f, k2[j], k1[j])) + k4[j], s[j]);
+            for(int j = 0; j < 12; ++j) s[j] = fmaf(h6, acc[j] + k[j], s[j]);
             if(s[6] < P.v_min || s[6] > P.v_max || s[7] < P.v_min || s[7] > P.v_max || s[8] < P.v_min || s[8] > P.v_max)
                 {
                     ok = false;
@@ -364,7 +367,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridV
 #pragma unroll
     for(int j = 0; j < 12; ++j) x1[j] = s[j];
     x1[12] = zc, x1[13] = lc, x1[14] = mc, x1[15] = nc;
-    x1[16] = h * (float)k;
+    x1[16] = h * (float)k_steps;
     cnt.steps = done;
     return ok;
 }

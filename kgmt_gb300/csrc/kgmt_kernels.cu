@@ -573,33 +573,51 @@ template <int NT>
 __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes)
 {
     const float F = (float)p.fine_cells;
+    constexpr int U = 4;  // regions whose loads are issued together
     for(int l = threadIdx.x; l < kScoreLanes; l += NT)
         {
             float acc = 0.0f;
-            for(uint32_t r = (uint32_t)l; r < p.regions; r += kScoreLanes)
+            for(uint32_t r0 = (uint32_t)l; r0 < p.regions; r0 += U * kScoreLanes)
                 {
-                    const uint64_t m = __ldcg(&p.marks[r]) | __ldcg(&p.newmarks[r]);
-                    p.marks[r] = m;
-                    p.newmarks[r] = 0ull;
-                    const int32_t nv = __ldcg(&p.valid[r]);
-                    float raw = 0.0f;  // adds nothing to the total
-                    float keep = -1.0f;  // marks "no valid sample" for the normalisation pass
-                    if(nv > 0)
+                    uint64_t m[U];
+                    int32_t nv[U], n[U];
+#pragma unroll
+                    for(int k = 0; k < U; ++k)
                         {
-                            const int32_t n = __ldcg(&p.counter[r]);
-                            const float cov = (float)__popcll(m) / F;
-                            const float a = p.epsilon + (float)nv;
-                            const float b = a + (float)(n - nv);
-                            const float fv = (a / b) * p.cell_volume;
-                            const float f2 = fv * fv;
-                            const float f4 = f2 * f2;
-                            const float nf = (float)n;
-                            const float den = (1.0f + cov) * (1.0f + nf * nf);
-                            raw = f4 / den;
-                            keep = raw;
+                            const uint32_t r = r0 + k * kScoreLanes;
+                            if(r < p.regions)
+                                {
+                                    m[k] = __ldcg(&p.marks[r]) | __ldcg(&p.newmarks[r]);
+                                    nv[k] = __ldcg(&p.valid[r]);
+                                    n[k] = __ldcg(&p.counter[r]);
+                                }
                         }
-                    p.score[r] = keep;
-                    acc = acc + raw;
+                    // regions in increasing order: the lane's sum keeps its fixed order
+#pragma unroll
+                    for(int k = 0; k < U; ++k)
+                        {
+                            const uint32_t r = r0 + k * kScoreLanes;
+                            if(r >= p.regions) break;
+                            p.marks[r] = m[k];
+                            p.newmarks[r] = 0ull;
+                            float raw = 0.0f;    // adds nothing to the total
+                            float keep = -1.0f;  // marks "no valid sample" for the normalisation pass
+                            if(nv[k] > 0)
+                                {
+                                    const float cov = (float)__popcll(m[k]) / F;
+                                    const float a = p.epsilon + (float)nv[k];
+                                    const float b = a + (float)(n[k] - nv[k]);
+                                    const float fv = (a / b) * p.cell_volume;
+                                    const float f2 = fv * fv;
+                                    const float f4 = f2 * f2;
+                                    const float nf = (float)n[k];
+                                    const float den = (1.0f + cov) * (1.0f + nf * nf);
+                                    raw = f4 / den;
+                                    keep = raw;
+                                }
+                            p.score[r] = keep;
+                            acc = acc + raw;
+                        }
                 }
             lanes[l] = acc;
         }
