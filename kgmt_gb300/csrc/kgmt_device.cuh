@@ -155,12 +155,14 @@ __device__ __forceinline__ bool box_hit(const float4* __restrict__ obs, uint32_t
     return !sep;
 }
 
-// Cell coordinate on the obstacle grid; monotone in x (every float operation
-// is), so a point inside both a box and the step box lies in a cell both
-// cell ranges contain -- culling by cells never drops a hit.
+// Cell coordinate on the obstacle grid; monotone in x (a subtraction and a
+// multiply by the positive grid_scale), and the grid is built with the same
+// function, so a point inside both a box and the step box lies in a cell both
+// cell ranges contain -- culling by cells never drops a hit.  (Region ids use
+// the reference's division instead; the culling grid is internal.)
 __device__ __forceinline__ int grid_cell(const QueryParams& P, float x)
 {
-    return cell_index(((float)P.grid_dim * (x - P.ws_min)) / P.ws_range, (int)P.grid_dim);
+    return cell_index((x - P.ws_min) * P.grid_scale, (int)P.grid_dim);
 }
 
 // Where the culling grid of the current query lives: its starts (and the

@@ -245,6 +245,7 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
     p.n_obstacles = n_obstacles;
     p.tiles_per_chain = L.tiles_per_chain;
     p.grid_dim = kGridDim;
+    p.grid_scale = (float)kGridDim / p.ws_range;
     p.grid_budget = L.grid_budget;
     if(chunk == nullptr)  // parameters only (function-level propagation): no buffers, no grid
         {

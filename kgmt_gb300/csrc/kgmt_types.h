@@ -99,6 +99,7 @@ struct QueryParams {
     // (built on the device at admission); lets a step box test only the boxes
     // of the cells it overlaps
     uint32_t grid_dim;       // cells per axis
+    float grid_scale;        // grid_dim / workspace size
     uint32_t grid_budget;    // capacity of grid_items (<= 65535)
     uint32_t* grid_meta;     // [4]: [0] items in use, [1] 1 = usable
     uint16_t* grid_start;    // [grid_dim^3 + 1] CSR starts (16-bit: at most 65535 items)
