@@ -84,6 +84,25 @@ __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
 }
 
 // ---------------------------------------------------------------------------
+// x / 6 rounded exactly as the IEEE division, as one multiply and one fused
+// multiply-add: RN(c_hi * x + RN(c_lo * x)) with c_hi = RN(1/6), c_lo =
+// RN(1/6 - c_hi) (Brisebarre & Muller, "Correctly rounded multiplication by
+// arbitrary precision constants", IEEE TC 2008).  Checked exhaustively over a
+// binade (tests/test_arith_cpu.py); the identity scales by powers of two, so
+// it holds for every finite |x| > 2^-98.  Elsewhere the true division runs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float div6(float x)
+{
+    const float ax = fabsf(x);
+    if(ax > 0x1p-98f && ax <= 0x1.fffffep127f) return fmaf(0x1.555556p-3f, x, -0x1.555556p-28f * x);
+    return x / 6.0f;
+}
+
+// x / d for a divisor that may be an exact power of two: then the product
+// with the exact reciprocal is the same IEEE result, without a division
+__device__ __forceinline__ float div_maybe_pow2(float x, float d, float inv_d, bool pow2) { return pow2 ? x * inv_d : x / d; }
+
+// ---------------------------------------------------------------------------
 // Regions on workspace-only grids.  r1 = (ix*L + iy)*L + iz (z least
 // significant, Graph.cu:105-113); the fine cell is located relative to the
 // exact corner ws_min + idx * cell_size.
@@ -105,17 +124,18 @@ __device__ __forceinline__ CellIds cell_ids(const QueryParams& P, float x, float
 {
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
-    int ix = cell_index((Lf * (x - P.ws_min)) / P.ws_range, L);
-    int iy = cell_index((Lf * (y - P.ws_min)) / P.ws_range, L);
-    int iz = cell_index((Lf * (z - P.ws_min)) / P.ws_range, L);
+    const bool rp = P.range_pow2 != 0, cp = P.cell_pow2 != 0;
+    int ix = cell_index(div_maybe_pow2(Lf * (x - P.ws_min), P.ws_range, P.inv_range, rp), L);
+    int iy = cell_index(div_maybe_pow2(Lf * (y - P.ws_min), P.ws_range, P.inv_range, rp), L);
+    int iz = cell_index(div_maybe_pow2(Lf * (z - P.ws_min), P.ws_range, P.inv_range, rp), L);
     const float Ff = (float)P.fine_len;
     const int F = (int)P.fine_len;
     float mx = P.ws_min + (float)ix * P.cell_size;
     float my = P.ws_min + (float)iy * P.cell_size;
     float mz = P.ws_min + (float)iz * P.cell_size;
-    int jx = cell_index((Ff * (x - mx)) / P.cell_size, F);
-    int jy = cell_index((Ff * (y - my)) / P.cell_size, F);
-    int jz = cell_index((Ff * (z - mz)) / P.cell_size, F);
+    int jx = cell_index(div_maybe_pow2(Ff * (x - mx), P.cell_size, P.inv_cell, cp), F);
+    int jy = cell_index(div_maybe_pow2(Ff * (y - my), P.cell_size, P.inv_cell, cp), F);
+    int jz = cell_index(div_maybe_pow2(Ff * (z - mz), P.cell_size, P.inv_cell, cp), F);
     return {(ix * L + iy) * L + iz, (jx * F + jy) * F + jz};
 }
 
@@ -123,9 +143,10 @@ __device__ __forceinline__ int region_of(const QueryParams& P, float x, float y,
 {
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
-    int ix = cell_index((Lf * (x - P.ws_min)) / P.ws_range, L);
-    int iy = cell_index((Lf * (y - P.ws_min)) / P.ws_range, L);
-    int iz = cell_index((Lf * (z - P.ws_min)) / P.ws_range, L);
+    const bool rp = P.range_pow2 != 0;
+    int ix = cell_index(div_maybe_pow2(Lf * (x - P.ws_min), P.ws_range, P.inv_range, rp), L);
+    int iy = cell_index(div_maybe_pow2(Lf * (y - P.ws_min), P.ws_range, P.inv_range, rp), L);
+    int iz = cell_index(div_maybe_pow2(Lf * (z - P.ws_min), P.ws_range, P.inv_range, rp), L);
     return (ix * L + iy) * L + iz;
 }
 
@@ -254,10 +275,10 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const GridVie
                     float half = v[d] + (a[d] * h) / 2.0f;
                     float full = v[d] + a[d] * h;
                     float sum = ref_rule ? v[d] + ((v[d] + 2.0f * half) + full) : ((v[d] + 2.0f * half) + 2.0f * half) + full;
-                    p[d] = p[d] + (sum * h) / 6.0f;
+                    p[d] = p[d] + div6(sum * h);
                 }
 #pragma unroll
-            for(int d = 0; d < 3; ++d) v[d] = v[d] + ((((a[d] + 2.0f * a[d]) + 2.0f * a[d]) + a[d]) * h) / 6.0f;
+            for(int d = 0; d < 3; ++d) v[d] = v[d] + div6((((a[d] + 2.0f * a[d]) + 2.0f * a[d]) + a[d]) * h);
             if(v[0] < P.v_min || v[0] > P.v_max || v[1] < P.v_min || v[1] > P.v_max || v[2] < P.v_min || v[2] > P.v_max)
                 {
                     ok = false;

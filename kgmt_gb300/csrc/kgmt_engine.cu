@@ -210,6 +210,15 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
     p.ws_range = range;
     p.cell_size = cell;
     p.cell_volume = cell2 * cell;
+    // a power of two divides exactly like a multiply by its reciprocal
+    auto pow2 = [](float v) {
+        int e = 0;
+        return v > 0.0f && std::isfinite(v) && std::frexp(v, &e) == 0.5f && e > -125 && e < 126;
+    };
+    p.range_pow2 = pow2(range) ? 1 : 0;
+    p.cell_pow2 = pow2(cell) ? 1 : 0;
+    p.inv_range = p.range_pow2 ? 1.0f / range : 0.0f;
+    p.inv_cell = p.cell_pow2 ? 1.0f / cell : 0.0f;
     p.coarse_len = c.coarse_len;
     p.fine_len = c.fine_len;
     p.regions = c.coarse_len * c.coarse_len * c.coarse_len;

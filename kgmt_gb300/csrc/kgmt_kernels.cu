@@ -643,7 +643,7 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
 // launch picks the variant for the admitted mix, so a single-model batch
 // pays for one model's registers only
 template <int NT, int MODELS>
-__global__ void __launch_bounds__(NT, (MODELS == 1 ? 768 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+__global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
 {
     // dynamic shared memory: boxes | grid starts | grid items | grid meta

@@ -64,6 +64,8 @@ struct QueryParams {
     float step_size, half_step, sixth_step;
     float goal_radius, epsilon;
     float ws_min, ws_max, ws_range, cell_size, cell_volume;
+    float inv_range, inv_cell;     // exact reciprocals when the sizes are powers of two
+    int32_t range_pow2, cell_pow2; // 1: divide by multiplying with the reciprocal (same IEEE result)
     uint32_t coarse_len, fine_len, regions, fine_cells;
     float v_min, v_max;
     float u_min[4], u_span[4];

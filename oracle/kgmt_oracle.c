@@ -148,6 +148,30 @@ void ko_sincosf(float x, float* s_out, float* c_out)
     *c_out = c;
 }
 
+/* Checks, over every float of the binades [1, 2) and (-2, -1], that
+ * RN(c_hi * x + RN(c_lo * x)) (one fused multiply-add) equals the IEEE
+ * quotient x / 6, with c_hi = RN(1/6), c_lo = RN(1/6 - c_hi): the division
+ * replacement the CUDA kernels use.  The identity is invariant under scaling
+ * by powers of two while c_lo * x stays normal, so one binade proves it for
+ * all finite |x| > 2^-98.  Returns the number of mismatches. */
+long ko_check_div6(void)
+{
+    const float ch = 0x1.555556p-3f, cl = -0x1.555556p-28f;
+    long bad = 0;
+    for(uint32_t m = 0; m < (1u << 23); ++m)
+        {
+            uint32_t bits = 0x3f800000u | m;
+            float x;
+            memcpy(&x, &bits, 4);
+            for(int sg = 0; sg < 2; ++sg)
+                {
+                    float xx = sg ? -x : x;
+                    if(fmaf(ch, xx, cl * xx) != xx / 6.0f) ++bad;
+                }
+        }
+    return bad;
+}
+
 int ko_sample_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 17 : 10; }
 int ko_state_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 12 : 6; }
 

@@ -99,6 +99,8 @@ typedef struct ko_iter_trace {
 /* ---- building blocks ---- */
 void ko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 float ko_u01(uint32_t x);
+/* mismatches of the fused-multiply-add replacement of x / 6 over two binades */
+long ko_check_div6(void);
 void ko_sincosf(float x, float* s, float* c);
 int ko_sample_dim(int32_t model);
 int ko_state_dim(int32_t model);
