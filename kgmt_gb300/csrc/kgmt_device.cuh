@@ -90,13 +90,17 @@ __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
 // arbitrary precision constants", IEEE TC 2008).  Checked exhaustively over a
 // binade (tests/test_arith_cpu.py); the identity scales by powers of two, so
 // it holds for every finite |x| > 2^-98.  Elsewhere the true division runs.
+// A divergent branch costs about as much as the arithmetic it guards, so the
+// hot loops evaluate div6_fast for several values, combine the div6_exact
+// predicates and take one rarely-taken branch to redo them with the division.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float div6(float x)
+__device__ __forceinline__ float div6_fast(float x) { return fmaf(0x1.555556p-3f, x, -0x1.555556p-28f * x); }
+__device__ __forceinline__ bool div6_exact(float x)
 {
     const float ax = fabsf(x);
-    if(ax > 0x1p-98f && ax <= 0x1.fffffep127f) return fmaf(0x1.555556p-3f, x, -0x1.555556p-28f * x);
-    return x / 6.0f;
+    return ax > 0x1p-98f && ax <= 0x1.fffffep127f;
 }
+__device__ __forceinline__ float div6(float x) { return div6_exact(x) ? div6_fast(x) : x / 6.0f; }
 
 // x / d for a divisor that may be an exact power of two: then the product
 // with the exact reciprocal is the same IEEE result, without a division
@@ -120,22 +124,36 @@ struct CellIds {
     int r2;  // fine cell inside r1, [0, fine_len^3)
 };
 
+// t[i] / d for three values, one (query-uniform) branch for all three
+__device__ __forceinline__ void div3_maybe_pow2(float* t, float d, float inv_d, bool pow2)
+{
+    if(pow2)
+        {
+#pragma unroll
+            for(int i = 0; i < 3; ++i) t[i] = t[i] * inv_d;
+        }
+    else
+        {
+#pragma unroll
+            for(int i = 0; i < 3; ++i) t[i] = t[i] / d;
+        }
+}
+
 __device__ __forceinline__ CellIds cell_ids(const QueryParams& P, float x, float y, float z)
 {
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
-    const bool rp = P.range_pow2 != 0, cp = P.cell_pow2 != 0;
-    int ix = cell_index(div_maybe_pow2(Lf * (x - P.ws_min), P.ws_range, P.inv_range, rp), L);
-    int iy = cell_index(div_maybe_pow2(Lf * (y - P.ws_min), P.ws_range, P.inv_range, rp), L);
-    int iz = cell_index(div_maybe_pow2(Lf * (z - P.ws_min), P.ws_range, P.inv_range, rp), L);
+    float t[3] = {Lf * (x - P.ws_min), Lf * (y - P.ws_min), Lf * (z - P.ws_min)};
+    div3_maybe_pow2(t, P.ws_range, P.inv_range, P.range_pow2 != 0);
+    const int ix = cell_index(t[0], L), iy = cell_index(t[1], L), iz = cell_index(t[2], L);
     const float Ff = (float)P.fine_len;
     const int F = (int)P.fine_len;
     float mx = P.ws_min + (float)ix * P.cell_size;
     float my = P.ws_min + (float)iy * P.cell_size;
     float mz = P.ws_min + (float)iz * P.cell_size;
-    int jx = cell_index(div_maybe_pow2(Ff * (x - mx), P.cell_size, P.inv_cell, cp), F);
-    int jy = cell_index(div_maybe_pow2(Ff * (y - my), P.cell_size, P.inv_cell, cp), F);
-    int jz = cell_index(div_maybe_pow2(Ff * (z - mz), P.cell_size, P.inv_cell, cp), F);
+    float f[3] = {Ff * (x - mx), Ff * (y - my), Ff * (z - mz)};
+    div3_maybe_pow2(f, P.cell_size, P.inv_cell, P.cell_pow2 != 0);
+    const int jx = cell_index(f[0], F), jy = cell_index(f[1], F), jz = cell_index(f[2], F);
     return {(ix * L + iy) * L + iz, (jx * F + jy) * F + jz};
 }
 
@@ -143,11 +161,9 @@ __device__ __forceinline__ int region_of(const QueryParams& P, float x, float y,
 {
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
-    const bool rp = P.range_pow2 != 0;
-    int ix = cell_index(div_maybe_pow2(Lf * (x - P.ws_min), P.ws_range, P.inv_range, rp), L);
-    int iy = cell_index(div_maybe_pow2(Lf * (y - P.ws_min), P.ws_range, P.inv_range, rp), L);
-    int iz = cell_index(div_maybe_pow2(Lf * (z - P.ws_min), P.ws_range, P.inv_range, rp), L);
-    return (ix * L + iy) * L + iz;
+    float t[3] = {Lf * (x - P.ws_min), Lf * (y - P.ws_min), Lf * (z - P.ws_min)};
+    div3_maybe_pow2(t, P.ws_range, P.inv_range, P.range_pow2 != 0);
+    return (cell_index(t[0], L) * L + cell_index(t[1], L)) * L + cell_index(t[2], L);
 }
 
 __device__ __forceinline__ float goal_distance(float x, float y, float z, const QueryParams& P)
@@ -200,9 +216,26 @@ __device__ __forceinline__ uint32_t grid_item(const GridView& g, uint32_t j)
     return j < kSmemGridItems ? g.items_s[j] : __ldg(g.items_g + j);
 }
 
-// true when the step box [a, b] (per-axis min/max) hits no obstacle
+// Consecutive step boxes of a trajectory share an end point, so the grid cell
+// of each end point is computed once and carried into the next step.  Since
+// grid_cell is monotone, the cell range of a step box [min(a, b), max(a, b)]
+// is [min(cell(a), cell(b)), max(cell(a), cell(b))] per axis.
+struct StepCells {
+    int x, y, z;  // cell of the step's start point
+    bool ok;      // the start point has no NaN coordinate
+};
+
+__device__ __forceinline__ StepCells start_cells(const QueryParams& P, float x, float y, float z)
+{
+    return {grid_cell(P, x), grid_cell(P, y), grid_cell(P, z), !(isnan(x) || isnan(y) || isnan(z))};
+}
+
+// true when the step box [a, b] (per-axis min/max) hits no obstacle.  The grid
+// path tests the boxes listed in the cells the step box overlaps, cell by cell
+// (x, then y, then z); more than kGridMaxVisit cells, or a NaN end point, fall
+// back to testing every box.  sc: cells of a on entry, of b on return.
 __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& grid, const float4* __restrict__ obs, uint32_t n_obs,
-                                          float ax, float ay, float az, float bx, float by, float bz, PropCount& cnt)
+                                          float ax, float ay, float az, float bx, float by, float bz, StepCells& sc, PropCount& cnt)
 {
     if(n_obs == 0) return true;
     const float lx = ax > bx ? bx : ax, hx = ax > bx ? ax : bx;
@@ -210,12 +243,27 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
     const float lz = az > bz ? bz : az, hz = az > bz ? az : bz;
     if(grid.start != nullptr)
         {
-            const int x0 = grid_cell(P, lx), x1 = grid_cell(P, hx);
-            const int y0 = grid_cell(P, ly), y1 = grid_cell(P, hy);
-            const int z0 = grid_cell(P, lz), z1 = grid_cell(P, hz);
-            if((uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1)) <= kGridMaxVisit)
+            const StepCells a = sc;
+            sc = start_cells(P, bx, by, bz);
+            const int x0 = min(a.x, sc.x), x1 = max(a.x, sc.x);
+            const int y0 = min(a.y, sc.y), y1 = max(a.y, sc.y);
+            const int z0 = min(a.z, sc.z), z1 = max(a.z, sc.z);
+            const uint32_t n_cells = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1));
+            if(a.ok && sc.ok && n_cells <= kGridMaxVisit)
                 {
                     const int G = (int)P.grid_dim;
+                    if(n_cells == 1)
+                        {
+                            // the common case: both end points in one cell
+                            const int c = (x0 * G + y0) * G + z0;
+                            const uint32_t e = grid.start[c + 1];
+                            for(uint32_t j = grid.start[c]; j < e; ++j)
+                                {
+                                    ++cnt.tests;
+                                    if(box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
+                                }
+                            return true;
+                        }
                     for(int cx = x0; cx <= x1; ++cx)
                         for(int cy = y0; cy <= y1; ++cy)
                             for(int cz = z0; cz <= z1; ++cz)
@@ -263,33 +311,48 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const GridVie
     float v[3] = {x0[3], x0[4], x0[5]};
     const float a[3] = {a0, a1, a2};
     const bool ref_rule = P.di_rule == KGMT_DI_RULE_REFERENCE;
+    // the velocity increment is the same every step: ((a + 2a) + 2a + a) h / 6
+    float dv[3];
+#pragma unroll
+    for(int d = 0; d < 3; ++d) dv[d] = div6((((a[d] + 2.0f * a[d]) + 2.0f * a[d]) + a[d]) * h);
+    StepCells sc = start_cells(P, p[0], p[1], p[2]);
     bool ok = true;
     int done = 0;
     for(int i = 0; i < k; ++i)
         {
             ++done;
             const float q0 = p[0], q1 = p[1], q2 = p[2];
+            float x[3];
 #pragma unroll
             for(int d = 0; d < 3; ++d)
                 {
                     float half = v[d] + (a[d] * h) / 2.0f;
                     float full = v[d] + a[d] * h;
                     float sum = ref_rule ? v[d] + ((v[d] + 2.0f * half) + full) : ((v[d] + 2.0f * half) + 2.0f * half) + full;
-                    p[d] = p[d] + div6(sum * h);
+                    x[d] = sum * h;
+                }
+            if(div6_exact(x[0]) && div6_exact(x[1]) && div6_exact(x[2]))
+                {
+#pragma unroll
+                    for(int d = 0; d < 3; ++d) p[d] = p[d] + div6_fast(x[d]);
+                }
+            else
+                {
+#pragma unroll
+                    for(int d = 0; d < 3; ++d) p[d] = p[d] + x[d] / 6.0f;
                 }
 #pragma unroll
-            for(int d = 0; d < 3; ++d) v[d] = v[d] + div6((((a[d] + 2.0f * a[d]) + 2.0f * a[d]) + a[d]) * h);
-            if(v[0] < P.v_min || v[0] > P.v_max || v[1] < P.v_min || v[1] > P.v_max || v[2] < P.v_min || v[2] > P.v_max)
+            for(int d = 0; d < 3; ++d) v[d] = v[d] + dv[d];
+            // velocity bound, then workspace bound: either ends the sample here
+            const bool out = (v[0] < P.v_min) | (v[0] > P.v_max) | (v[1] < P.v_min) | (v[1] > P.v_max) | (v[2] < P.v_min) |
+                             (v[2] > P.v_max) | (p[0] < P.ws_min) | (p[0] > P.ws_max) | (p[1] < P.ws_min) | (p[1] > P.ws_max) |
+                             (p[2] < P.ws_min) | (p[2] > P.ws_max);
+            if(out)
                 {
                     ok = false;
                     break;
                 }
-            if(p[0] < P.ws_min || p[0] > P.ws_max || p[1] < P.ws_min || p[1] > P.ws_max || p[2] < P.ws_min || p[2] > P.ws_max)
-                {
-                    ok = false;
-                    break;
-                }
-            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], cnt))
+            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], sc, cnt))
                 {
                     ok = false;
                     break;
@@ -353,6 +416,7 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridV
     float s[12], k[12], t[12], acc[12];
 #pragma unroll
     for(int j = 0; j < 12; ++j) s[j] = x0[j];
+    StepCells sc = start_cells(P, s[0], s[1], s[2]);
     bool ok = true;
     int done = 0;
     for(int i = 0; i < k_steps; ++i)
@@ -371,17 +435,15 @@ __device__ __forceinline__ bool propagate_quad(const QueryParams& P, const GridV
             quad_ode(P, t, zc, lc, mc, nc, k);
 #pragma unroll
             for(int j = 0; j < 12; ++j) s[j] = fmaf(h6, acc[j] + k[j], s[j]);
-            if(s[6] < P.v_min || s[6] > P.v_max || s[7] < P.v_min || s[7] > P.v_max || s[8] < P.v_min || s[8] > P.v_max)
+            const bool out = (s[6] < P.v_min) | (s[6] > P.v_max) | (s[7] < P.v_min) | (s[7] > P.v_max) | (s[8] < P.v_min) |
+                             (s[8] > P.v_max) | (s[0] < P.ws_min) | (s[0] > P.ws_max) | (s[1] < P.ws_min) | (s[1] > P.ws_max) |
+                             (s[2] < P.ws_min) | (s[2] > P.ws_max);
+            if(out)
                 {
                     ok = false;
                     break;
                 }
-            if(s[0] < P.ws_min || s[0] > P.ws_max || s[1] < P.ws_min || s[1] > P.ws_max || s[2] < P.ws_min || s[2] > P.ws_max)
-                {
-                    ok = false;
-                    break;
-                }
-            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, s[0], s[1], s[2], cnt))
+            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, s[0], s[1], s[2], sc, cnt))
                 {
                     ok = false;
                     break;
