@@ -57,8 +57,11 @@ typedef enum kgmt_status {
     KGMT_ERR_INTERNAL = 8
 } kgmt_status;
 
-/* dynamics models, numbered like the reference's MODEL macro (config.h) */
+/* dynamics models, numbered like the reference's MODEL macro (config.h,
+ * statePropagator.cu:375-390) */
+#define KGMT_MODEL_UNICYCLE 0        /* planar: 2-D workspace, boxes [n][4] */
 #define KGMT_MODEL_DOUBLE_INTEGRATOR 1
+#define KGMT_MODEL_DUBINS_AIRPLANE 2
 #define KGMT_MODEL_QUADROTOR 3
 
 /* double-integrator position update */
@@ -75,12 +78,15 @@ typedef enum kgmt_status {
 #define KGMT_MAX_FINE_CELLS 64
 
 /* Runtime replacement for the reference's config.h macros.  Workspace-only
- * region grids: coarse_len^3 regions (W_R1_LENGTH), fine_len^3 cells per
- * region (W_R2_LENGTH, at most 64 cells).  Sample rows are state + control +
- * duration: 10 floats for the double integrator, 17 for the quadrotor
- * (SAMPLE_DIM).  Steps per sample k = min_steps + floor(u * (max_steps -
- * min_steps + 1)), duration = k * step_size (MAX_PROPAGATION_DURATION,
- * STEP_SIZE). */
+ * region grids: coarse_len^W regions (W_R1_LENGTH), fine_len^W cells per
+ * region (W_R2_LENGTH, at most 64 cells), W = 3, or 2 for the planar
+ * unicycle.  Sample rows are state + control + duration (SAMPLE_DIM):
+ *   unicycle          7: x y theta v | a steering dt               (statePropagator.cu:13-74)
+ *   double integrator 10: x y z vx vy vz | ax ay az | k*h           (76-142)
+ *   Dubins airplane   10: x y z yaw pitch v | yaw-rate pitch-rate a | k*h (147-244)
+ *   quadrotor         17: 12 states | Zc Lc Mc Nc | k*h             (246-370)
+ * Steps per sample k = min_steps + floor(u * (max_steps - min_steps + 1))
+ * (MAX_PROPAGATION_DURATION, STEP_SIZE). */
 typedef struct kgmt_config {
     int32_t model;             /* KGMT_MODEL_*                                 */
     int32_t di_rule;           /* KGMT_DI_RULE_*                               */
@@ -94,10 +100,15 @@ typedef struct kgmt_config {
     float epsilon;     /* EPSILON     */
     float ws_min, ws_max;
     uint32_t coarse_len, fine_len;
-    float v_min, v_max;
-    float u_min[4], u_max[4]; /* control bounds (DI: ax ay az; quad: Zc Lc Mc Nc) */
+    float v_min, v_max; /* V_MIN, V_MAX (not checked for the unicycle, as in the reference) */
+    /* control bounds, in the reference's draw order: DI ax ay az; quad Zc Lc
+     * Mc Nc; Dubins a, yaw rate, pitch rate; unicycle a, steering, dt */
+    float u_min[4], u_max[4];
     float nu, mu, ix, iy, iz, gravity, mass_inv; /* quadrotor constants */
     uint64_t seed; /* Philox key of this query */
+    float pitch_min, pitch_max; /* Dubins airplane pitch bounds (DUBINS_AIRPLANE_MIN/MAX_PITCH) */
+    float wheelbase;            /* unicycle length (UNI_LENGTH) */
+    uint32_t reserved;          /* zero */
 } kgmt_config;
 
 typedef struct kgmt_result {
@@ -132,8 +143,9 @@ KGMT_API int32_t kgmt_sample_dim(int32_t model);
 KGMT_API kgmt_status kgmt_create(const kgmt_config* cfg, void* stream, kgmt_planner** out);
 KGMT_API void kgmt_destroy(kgmt_planner* p);
 /* h_initial / h_goal: host rows of kgmt_sample_dim(model) floats (only the
- * first three goal components are used); d_obstacles: caller-owned device
- * array [n_obstacles][6].  Blocks until the plan is done. */
+ * first W goal components are used); d_obstacles: caller-owned device array
+ * [n_obstacles][2W] = min corner, max corner (W = 3; 2 for the unicycle).
+ * Blocks until the plan is done. */
 KGMT_API kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles, uint32_t n_obstacles);
 KGMT_API kgmt_status kgmt_get_result(const kgmt_planner* p, kgmt_result* out);
 /* copies the first min(tree_size, max_nodes) nodes; any pointer may be NULL */

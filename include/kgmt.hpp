@@ -26,11 +26,11 @@
 namespace kgmt {
 
 // Obstacle CSV of the reference (include/config/obstacles/*/obstacles.csv,
-// read by src/helper/helper.cu:13-39): comma-separated floats, six per box
-// (min x, min y, min z, max x, max y, max z), any line breaks.  Throws on an
-// unreadable file or a count that is not a multiple of six (the reference
-// exits the process).
-inline std::vector<float> read_obstacles_csv(const std::string& path)
+// read by src/helper/helper.cu:13-39): comma-separated floats, 2 * W per box
+// (min corner, max corner; W = workspace_dim, 3, or 2 for the unicycle), any
+// line breaks.  Throws on an unreadable file or a count that is not a
+// multiple of 2 * W (the reference exits the process).
+inline std::vector<float> read_obstacles_csv(const std::string& path, int workspace_dim = 3)
 {
     std::ifstream f(path);
     if(!f) throw std::runtime_error("kgmt: cannot open obstacle file " + path);
@@ -47,7 +47,9 @@ inline std::vector<float> read_obstacles_csv(const std::string& path)
                     out.push_back(std::stof(tok.substr(a)));
                 }
         }
-    if(out.size() % 6 != 0) throw std::runtime_error("kgmt: obstacle file " + path + " does not hold six values per box");
+    const size_t per_box = 2 * (size_t)workspace_dim;
+    if(out.size() % per_box != 0)
+        throw std::runtime_error("kgmt: obstacle file " + path + " does not hold " + std::to_string(per_box) + " values per box");
     return out;
 }
 

@@ -34,6 +34,7 @@ class KgmtConfig(C.Structure):
         ("coarse_len", C.c_uint32), ("fine_len", C.c_uint32), ("v_min", C.c_float), ("v_max", C.c_float),
         ("u_min", C.c_float * 4), ("u_max", C.c_float * 4), ("nu", C.c_float), ("mu", C.c_float), ("ix", C.c_float),
         ("iy", C.c_float), ("iz", C.c_float), ("gravity", C.c_float), ("mass_inv", C.c_float), ("seed", C.c_uint64),
+        ("pitch_min", C.c_float), ("pitch_max", C.c_float), ("wheelbase", C.c_float), ("reserved", C.c_uint32),
     ]
 
 

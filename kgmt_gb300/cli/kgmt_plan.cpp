@@ -43,7 +43,14 @@ int main(int argc, char** argv)
             std::string a = argv[i];
             const char* v = i + 1 < argc ? argv[i + 1] : nullptr;
             if(a == "--obstacles" && v) obstacles = v, ++i;
-            else if(a == "--model" && v) model = std::string(v) == "quad" ? KGMT_MODEL_QUADROTOR : KGMT_MODEL_DOUBLE_INTEGRATOR, ++i;
+            else if(a == "--model" && v)
+                {
+                    const std::string m = v;
+                    model = m == "quad" ? KGMT_MODEL_QUADROTOR
+                          : m == "dubins" ? KGMT_MODEL_DUBINS_AIRPLANE
+                          : m == "unicycle" ? KGMT_MODEL_UNICYCLE : KGMT_MODEL_DOUBLE_INTEGRATOR;
+                    ++i;
+                }
             else if(a == "--init" && v) init = parse3(v), ++i;
             else if(a == "--goal" && v) goal = parse3(v), ++i;
             else if(a == "--seed" && v) seed = std::atoll(v), ++i;
@@ -53,7 +60,7 @@ int main(int argc, char** argv)
             else if(a == "--out" && v) out = v, ++i;
             else
                 {
-                    std::fprintf(stderr, "usage: %s --obstacles scene.csv [--model di|quad] [--init x,y,z] [--goal x,y,z] "
+                    std::fprintf(stderr, "usage: %s --obstacles scene.csv [--model di|quad|dubins|unicycle] [--init x,y,z] [--goal x,y,z] "
                                          "[--seed N] [--capacity N] [--iterations N] [--repeat N] [--out DIR]\n", argv[0]);
                     return 2;
                 }
@@ -64,8 +71,11 @@ int main(int argc, char** argv)
             cfg.seed = (uint64_t)seed;
             if(capacity > 0) cfg.tree_capacity = (uint32_t)capacity;
             if(iterations > 0) cfg.max_iterations = (uint32_t)iterations;
-            std::vector<float> obs = obstacles.empty() ? std::vector<float>() : kgmt::read_obstacles_csv(obstacles);
-            const uint32_t n = (uint32_t)(obs.size() / 6);
+            // the unicycle is planar: rows of four (min x, min y, max x, max y); its
+            // --init / --goal third value is the heading (ignored for the goal)
+            const int W = model == KGMT_MODEL_UNICYCLE ? 2 : 3;
+            std::vector<float> obs = obstacles.empty() ? std::vector<float>() : kgmt::read_obstacles_csv(obstacles, W);
+            const uint32_t n = (uint32_t)(obs.size() / (2 * W));
             float* d_obs = nullptr;
             if(n)
                 {

@@ -40,7 +40,7 @@ extern "C" const char* kgmt_last_error(void) { return kgmt::g_last_error.c_str()
 
 extern "C" int32_t kgmt_sample_dim(int32_t model)
 {
-    if(model != KGMT_MODEL_DOUBLE_INTEGRATOR && model != KGMT_MODEL_QUADROTOR) return -1;
+    if(model < KGMT_MODEL_UNICYCLE || model > KGMT_MODEL_QUADROTOR) return -1;
     return (int32_t)sample_dim_of(model);
 }
 
@@ -64,6 +64,9 @@ extern "C" kgmt_status kgmt_config_default(int32_t model, kgmt_config* out)
     c.iz = 2.0f;
     c.mass_inv = 1.0f;
     c.seed = 1;
+    c.pitch_min = -3.14159265358979323846f / 3.0f;
+    c.pitch_max = 3.14159265358979323846f / 3.0f;
+    c.wheelbase = 1.0f;
     if(model == KGMT_MODEL_DOUBLE_INTEGRATOR)
         {
             c.tree_capacity = 100000;
@@ -91,6 +94,40 @@ extern "C" kgmt_status kgmt_config_default(int32_t model, kgmt_config* out)
             c.u_min[0] = 0.0f, c.u_max[0] = 0.3f;
             for(int i = 1; i < 4; ++i) c.u_min[i] = -pi, c.u_max[i] = pi;
             c.gravity = -0.0981f;
+        }
+    else if(model == KGMT_MODEL_DUBINS_AIRPLANE)
+        {
+            // the reference's Dubins airplane block of config.h (workspace-only grid)
+            const float pi = 3.14159265358979323846f;
+            c.tree_capacity = 200000;
+            c.samples_per_node = 4;
+            c.max_iterations = 300;
+            c.min_steps = 1;
+            c.max_steps = 10;
+            c.step_size = 0.1f;
+            c.coarse_len = 8;
+            c.fine_len = 2;
+            c.v_min = 0.0f;
+            c.v_max = 0.3f;
+            c.u_min[0] = -0.3f, c.u_max[0] = 0.3f;                    // a
+            c.u_min[1] = -pi / 4.0f, c.u_max[1] = pi / 4.0f;          // yaw rate
+            c.u_min[2] = -pi / 4.0f, c.u_max[2] = pi / 4.0f;          // pitch rate
+        }
+    else if(model == KGMT_MODEL_UNICYCLE)
+        {
+            // the reference's unicycle constants (config.h UNI_*), planar unit square
+            const float pi = 3.14159265358979323846f;
+            c.tree_capacity = 100000;
+            c.samples_per_node = 4;
+            c.max_iterations = 200;
+            c.min_steps = 1;
+            c.max_steps = 10;
+            c.step_size = 0.1f;
+            c.coarse_len = 8;
+            c.fine_len = 4;
+            c.u_min[0] = -0.2f, c.u_max[0] = 0.2f;                    // a
+            c.u_min[1] = -pi / 2.0f, c.u_max[1] = pi / 2.0f;          // steering
+            c.u_min[2] = 0.1f, c.u_max[2] = 2.0f;                     // dt (UNI_MIN_DT, UNI_MAX_DT)
         }
     else
         {
@@ -171,7 +208,8 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
     size_t off = 0;
     RETURN_IF(!p->arena.alloc(L.total, &off), KGMT_ERR_OOM, "kgmt_plan: arena allocation failed");
     p->params = make_params(p->cfg, h_initial, h_goal, p->arena.base() + off, L, nullptr, n_obstacles);
-    CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, p->params.obstacles, n_obstacles, p->eng.stream()), "stage obstacles"));
+    CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, p->params.obstacles, n_obstacles, (int)ws_dims_of(p->cfg.model), p->eng.stream()),
+                         "stage obstacles"));
     p->eng.host_params(0) = p->params;
     p->eng.set_models(Engine::model_bit(p->cfg.model));
     CHECK_ST(p->eng.admit(0, 1, 1));
@@ -349,7 +387,7 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     for(uint32_t i = 0; i < n; ++i)
         {
             const QueryState& q = b->states[i];
-            const uint64_t per_step = cfgs[i].model == KGMT_MODEL_QUADROTOR ? kOpsPerStepQuad : kOpsPerStepDI;
+            const uint64_t per_step = ops_per_step(cfgs[i].model);
             s.steps_executed += q.steps;
             s.obstacle_tests += q.tests;
             s.samples += q.samples_drawn;
@@ -389,7 +427,7 @@ extern "C" kgmt_status kgmt_plan_batch(kgmt_batch* b, uint32_t n, const kgmt_con
     if(boxes)
         {
             CHECK_ST(cuda_status(cudaMemcpyAsync(raw, h_obstacles, (size_t)boxes * 24, cudaMemcpyHostToDevice, s), "upload obstacles"));
-            CHECK_ST(cuda_status(launch_stage_obstacles(raw, region, boxes, s), "stage obstacles"));
+            CHECK_ST(cuda_status(launch_stage_obstacles(raw, region, boxes, 3, s), "stage obstacles"));
             b->eng.add_launches(1);
         }
     return batch_run(b, n, cfgs, nullptr, nullptr, results);
@@ -408,7 +446,7 @@ extern "C" kgmt_status kgmt_plan_batch_device(kgmt_batch* b, uint32_t n, const k
     RETURN_IF(boxes > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan_batch_device: obstacles pointer is NULL");
     if(boxes)
         {
-            CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, region, boxes, b->eng.stream()), "stage obstacles"));
+            CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, region, boxes, 3, b->eng.stream()), "stage obstacles"));
             b->eng.add_launches(1);
         }
     return batch_run(b, n, cfgs, d_inits, d_goals, results);
@@ -562,7 +600,7 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
                     float* raw = (float*)(chunk + raw_at);
                     CHECK_ST(cuda_status(cudaMemcpyAsync(raw, q.obstacles.data(), (size_t)n_obs * 24, cudaMemcpyHostToDevice, st),
                                          "upload obstacles"));
-                    CHECK_ST(cuda_status(launch_stage_obstacles(raw, prm.obstacles, n_obs, st), "stage obstacles"));
+                    CHECK_ST(cuda_status(launch_stage_obstacles(raw, prm.obstacles, n_obs, 3, st), "stage obstacles"));
                 }
             s->eng.host_params(slot) = prm;
             CHECK_ST(s->eng.upload_params(slot, 1));

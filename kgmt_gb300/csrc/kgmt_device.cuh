@@ -139,8 +139,14 @@ __device__ __forceinline__ void div3_maybe_pow2(float* t, float d, float inv_d, 
         }
 }
 
-__device__ __forceinline__ CellIds cell_ids(const QueryParams& P, float x, float y, float z)
+// Workspace position of a sample row: x y z, or x y and a z pinned to ws_min
+// for the planar unicycle (whose third component is its heading).  Planar
+// regions drop the z digit: r1 = ix*L + iy, fine cell jx*F + jy.
+__device__ __forceinline__ float row_z(const QueryParams& P, const float* x) { return P.planar ? P.ws_min : x[2]; }
+
+__device__ __forceinline__ CellIds cell_ids(const QueryParams& P, const float* row)
 {
+    const float x = row[0], y = row[1], z = row_z(P, row);
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
     float t[3] = {Lf * (x - P.ws_min), Lf * (y - P.ws_min), Lf * (z - P.ws_min)};
@@ -154,22 +160,30 @@ __device__ __forceinline__ CellIds cell_ids(const QueryParams& P, float x, float
     float f[3] = {Ff * (x - mx), Ff * (y - my), Ff * (z - mz)};
     div3_maybe_pow2(f, P.cell_size, P.inv_cell, P.cell_pow2 != 0);
     const int jx = cell_index(f[0], F), jy = cell_index(f[1], F), jz = cell_index(f[2], F);
+    if(P.planar) return {ix * L + iy, jx * F + jy};
     return {(ix * L + iy) * L + iz, (jx * F + jy) * F + jz};
 }
 
-__device__ __forceinline__ int region_of(const QueryParams& P, float x, float y, float z)
+__device__ __forceinline__ int region_of(const QueryParams& P, const float* row)
 {
     const float Lf = (float)P.coarse_len;
     const int L = (int)P.coarse_len;
-    float t[3] = {Lf * (x - P.ws_min), Lf * (y - P.ws_min), Lf * (z - P.ws_min)};
+    float t[3] = {Lf * (row[0] - P.ws_min), Lf * (row[1] - P.ws_min), Lf * (row_z(P, row) - P.ws_min)};
     div3_maybe_pow2(t, P.ws_range, P.inv_range, P.range_pow2 != 0);
-    return (cell_index(t[0], L) * L + cell_index(t[1], L)) * L + cell_index(t[2], L);
+    const int ixy = cell_index(t[0], L) * L + cell_index(t[1], L);
+    return P.planar ? ixy : ixy * L + cell_index(t[2], L);
 }
 
-__device__ __forceinline__ float goal_distance(float x, float y, float z, const QueryParams& P)
+// helper.cuh:138-152 (distance over the W workspace components)
+__device__ __forceinline__ float goal_distance(const QueryParams& P, const float* row)
 {
-    float dx = x - P.goal[0], dy = y - P.goal[1], dz = z - P.goal[2];
-    float s = (dx * dx + dy * dy) + dz * dz;
+    float dx = row[0] - P.goal[0], dy = row[1] - P.goal[1];
+    float s = dx * dx + dy * dy;
+    if(!P.planar)
+        {
+            float dz = row[2] - P.goal[2];
+            s = s + dz * dz;
+        }
     return sqrtf(s);
 }
 
@@ -189,6 +203,15 @@ __device__ __forceinline__ bool box_hit(const float4* __restrict__ obs, uint32_t
     const float4 mn = obs[2 * o];
     const float4 mx = obs[2 * o + 1];
     const bool sep = (hx <= mn.x) | (mx.x <= lx) | (hy <= mn.y) | (mx.y <= ly) | (hz <= mn.z) | (mx.z <= lz);
+    return !sep;
+}
+
+// planar workspace (W_DIM 2): the z extents play no part
+__device__ __forceinline__ bool box_hit_xy(const float4* __restrict__ obs, uint32_t o, float lx, float ly, float hx, float hy)
+{
+    const float4 mn = obs[2 * o];
+    const float4 mx = obs[2 * o + 1];
+    const bool sep = (hx <= mn.x) | (mx.x <= lx) | (hy <= mn.y) | (mx.y <= ly);
     return !sep;
 }
 
@@ -234,6 +257,8 @@ __device__ __forceinline__ StepCells start_cells(const QueryParams& P, float x, 
 // path tests the boxes listed in the cells the step box overlaps, cell by cell
 // (x, then y, then z); more than kGridMaxVisit cells, or a NaN end point, fall
 // back to testing every box.  sc: cells of a on entry, of b on return.
+// PLANAR: z is ignored (a and b carry z = ws_min, grid cell 0).
+template <bool PLANAR = false>
 __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& grid, const float4* __restrict__ obs, uint32_t n_obs,
                                           float ax, float ay, float az, float bx, float by, float bz, StepCells& sc, PropCount& cnt)
 {
@@ -260,7 +285,7 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
                             for(uint32_t j = grid.start[c]; j < e; ++j)
                                 {
                                     ++cnt.tests;
-                                    if(box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
+                                    if(PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
                                 }
                             return true;
                         }
@@ -273,14 +298,14 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
                                     for(uint32_t j = grid.start[c]; j < e; ++j)
                                         {
                                             ++cnt.tests;
-                                            if(box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
+                                            if(PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
                                         }
                                 }
                     return true;
                 }
         }
     bool hit = false;
-    for(uint32_t o = 0; o < n_obs; ++o) hit |= box_hit(obs, o, lx, ly, lz, hx, hy, hz);
+    for(uint32_t o = 0; o < n_obs; ++o) hit |= PLANAR ? box_hit_xy(obs, o, lx, ly, hx, hy) : box_hit(obs, o, lx, ly, lz, hx, hy, hz);
     cnt.tests += n_obs;
     return !hit;
 }
@@ -362,6 +387,125 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const GridVie
     x1[3] = v[0], x1[4] = v[1], x1[5] = v[2];
     x1[6] = a0, x1[7] = a1, x1[8] = a2;
     x1[9] = h * (float)k;
+    cnt.steps = done;
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Dubins airplane (statePropagator.cu:147-244): state [x y z yaw pitch v],
+// controls drawn as a, yaw rate, pitch rate; row [x y z yaw pitch v | yr pr
+// a | k*h].  Yaw and pitch are linear in time within a step and v is linear,
+// so the RK4 stages are closed-form: with A the midpoint term,
+//   x += (h/6) * ((v cos p) cos y + 2 (A + A) + B)
+// in the reference's order (the midpoint stages k2 = k3 coincide).  The end
+// stage's attitude is the next step's start attitude (same float operation),
+// so its sine and cosine are carried over.  Checks in the reference's order:
+// speed, pitch, workspace, obstacles.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool propagate_dubins(const QueryParams& P, const GridView& grid, const float* x0, const float* u, const float4* obs,
+                                                 uint32_t n_obs, float* x1, PropCount& cnt)
+{
+    const float a = P.u_min[0] + u[0] * P.u_span[0];
+    const float yr = P.u_min[1] + u[1] * P.u_span[1];
+    const float pr = P.u_min[2] + u[2] * P.u_span[2];
+    const int k = draw_steps(P, u[3]);
+    const float h = P.step_size, hh = P.half_step, h6 = P.sixth_step;
+    float x = x0[0], y = x0[1], z = x0[2], yaw = x0[3], pitch = x0[4], v = x0[5];
+    const float dvm = hh * a, dve = h * a;               // 0.5 h a, h a
+    const float dpm = hh * pr, dym = hh * yr;            // midpoint attitude offsets
+    const float dpe = h * pr, dye = h * yr;              // end attitude offsets
+    const float dv = h6 * ((a + 2.0f * (a + a)) + a);    // (h/6)(a + 2(a + a) + a)
+    float sp, cp, sy, cy;
+    sincos_portable(pitch, sp, cp);
+    sincos_portable(yaw, sy, cy);
+    StepCells sc = start_cells(P, x, y, z);
+    bool ok = true;
+    int done = 0;
+    for(int i = 0; i < k; ++i)
+        {
+            ++done;
+            const float q0 = x, q1 = y, q2 = z;
+            float spm, cpm, sym, cym, spe, cpe, sye, cye;
+            sincos_portable(pitch + dpm, spm, cpm);
+            sincos_portable(yaw + dym, sym, cym);
+            sincos_portable(pitch + dpe, spe, cpe);
+            sincos_portable(yaw + dye, sye, cye);
+            const float vm = v + dvm, ve = v + dve;
+            const float ax = (vm * cpm) * cym, bx = (ve * cpe) * cye;
+            const float ay = (vm * cpm) * sym, by = (ve * cpe) * sye;
+            const float az = vm * spm, bz = ve * spe;
+            x = x + h6 * ((((v * cp) * cy) + 2.0f * (ax + ax)) + bx);
+            y = y + h6 * ((((v * cp) * sy) + 2.0f * (ay + ay)) + by);
+            z = z + h6 * (((v * sp) + 2.0f * (az + az)) + bz);
+            yaw = yaw + dye;
+            pitch = pitch + dpe;
+            v = v + dv;
+            sp = spe, cp = cpe, sy = sye, cy = cye;
+            const bool out = (v < P.v_min) | (v > P.v_max) | (pitch < P.pitch_min) | (pitch > P.pitch_max) | (x < P.ws_min) | (x > P.ws_max) |
+                             (y < P.ws_min) | (y > P.ws_max) | (z < P.ws_min) | (z > P.ws_max);
+            if(out)
+                {
+                    ok = false;
+                    break;
+                }
+            if(!step_free(P, grid, obs, n_obs, q0, q1, q2, x, y, z, sc, cnt))
+                {
+                    ok = false;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = z, x1[3] = yaw, x1[4] = pitch, x1[5] = v;
+    x1[6] = yr, x1[7] = pr, x1[8] = a;
+    x1[9] = h * (float)k;
+    cnt.steps = done;
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Unicycle (statePropagator.cu:13-74), planar: state [x y theta v], controls
+// drawn as a, steering, dt; row [x y theta v | a steering dt].  Explicit Euler
+// in the reference's order; tan(steering) is the same every step and is taken
+// as sin/cos of the portable pair.  Checks: workspace (x, y), then obstacles
+// in the plane (there is no speed check in the reference).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool propagate_unicycle(const QueryParams& P, const GridView& grid, const float* x0, const float* u, const float4* obs,
+                                                   uint32_t n_obs, float* x1, PropCount& cnt)
+{
+    const float a = P.u_min[0] + u[0] * P.u_span[0];
+    const float steer = P.u_min[1] + u[1] * P.u_span[1];
+    const float dt = P.u_min[2] + u[2] * P.u_span[2];
+    const int k = draw_steps(P, u[3]);
+    const float h = P.step_size, zw = P.ws_min;
+    float x = x0[0], y = x0[1], th = x0[2], v = x0[3];
+    float ss, cs;
+    sincos_portable(steer, ss, cs);
+    const float tan_steer = ss / cs;
+    StepCells sc = start_cells(P, x, y, zw);
+    bool ok = true;
+    int done = 0;
+    for(int i = 0; i < k; ++i)
+        {
+            ++done;
+            const float q0 = x, q1 = y;
+            float st, ct;
+            sincos_portable(th, st, ct);
+            x = x + (v * ct) * h;
+            y = y + (v * st) * h;
+            th = th + ((v / P.wheelbase) * tan_steer) * h;
+            v = v + a * h;
+            if((x < P.ws_min) | (x > P.ws_max) | (y < P.ws_min) | (y > P.ws_max))
+                {
+                    ok = false;
+                    break;
+                }
+            if(!step_free<true>(P, grid, obs, n_obs, q0, q1, zw, x, y, zw, sc, cnt))
+                {
+                    ok = false;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = th, x1[3] = v;
+    x1[4] = a, x1[5] = steer, x1[6] = dt;
     cnt.steps = done;
     return ok;
 }

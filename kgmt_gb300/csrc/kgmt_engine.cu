@@ -116,7 +116,14 @@ void DeviceArena::reset()
 // ---------------------------------------------------------------------------
 // layout / params
 // ---------------------------------------------------------------------------
-uint32_t sample_dim_of(int32_t model) { return model == KGMT_MODEL_QUADROTOR ? 17u : 10u; }
+// SAMPLE_DIM per model: unicycle 7, double integrator 10, Dubins airplane 10, quadrotor 17
+uint32_t sample_dim_of(int32_t model) { return model == KGMT_MODEL_QUADROTOR ? 17u : model == KGMT_MODEL_UNICYCLE ? 7u : 10u; }
+// workspace dimension W (W_DIM): 2 for the planar unicycle
+uint32_t ws_dims_of(int32_t model) { return model == KGMT_MODEL_UNICYCLE ? 2u : 3u; }
+uint32_t regions_of(const kgmt_config& c)
+{
+    return ws_dims_of(c.model) == 2 ? c.coarse_len * c.coarse_len : c.coarse_len * c.coarse_len * c.coarse_len;
+}
 
 kgmt_status validate_config(const kgmt_config& c)
 {
@@ -124,7 +131,7 @@ kgmt_status validate_config(const kgmt_config& c)
         set_error(std::string("invalid config: ") + m);
         return KGMT_ERR_INVALID_ARG;
     };
-    if(c.model != KGMT_MODEL_DOUBLE_INTEGRATOR && c.model != KGMT_MODEL_QUADROTOR) return bad("model");
+    if(c.model < KGMT_MODEL_UNICYCLE || c.model > KGMT_MODEL_QUADROTOR) return bad("model");
     if(c.di_rule != KGMT_DI_RULE_RK4 && c.di_rule != KGMT_DI_RULE_REFERENCE) return bad("di_rule");
     if(c.tree_capacity < 2 || c.tree_capacity > (1u << 28)) return bad("tree_capacity must be in [2, 2^28]");
     if(c.samples_per_node < 1 || c.samples_per_node > 1024) return bad("samples_per_node must be in [1, 1024]");
@@ -133,10 +140,13 @@ kgmt_status validate_config(const kgmt_config& c)
     if(!(c.step_size > 0.0f) || !std::isfinite(c.step_size)) return bad("step_size");
     if(!(c.ws_max > c.ws_min)) return bad("ws_max must exceed ws_min");
     if(c.coarse_len < 1 || c.coarse_len > 128) return bad("coarse_len must be in [1, 128]");
-    if(c.fine_len < 1 || c.fine_len * c.fine_len * c.fine_len > KGMT_MAX_FINE_CELLS) return bad("fine_len^3 must be in [1, 64]");
+    const uint32_t fine_cells = ws_dims_of(c.model) == 2 ? c.fine_len * c.fine_len : c.fine_len * c.fine_len * c.fine_len;
+    if(c.fine_len < 1 || c.fine_len > 8 || fine_cells > KGMT_MAX_FINE_CELLS) return bad("fine_len^W must be in [1, 64]");
     if(!(c.v_max >= c.v_min)) return bad("v_max < v_min");
     if(!(c.goal_radius >= 0.0f) || !(c.epsilon >= 0.0f)) return bad("goal_radius / epsilon");
     if(c.model == KGMT_MODEL_QUADROTOR && (c.ix == 0.0f || c.iy == 0.0f || c.iz == 0.0f)) return bad("inertia must be non-zero");
+    if(c.model == KGMT_MODEL_DUBINS_AIRPLANE && !(c.pitch_max >= c.pitch_min)) return bad("pitch_max < pitch_min");
+    if(c.model == KGMT_MODEL_UNICYCLE && (c.wheelbase == 0.0f || !std::isfinite(c.wheelbase))) return bad("wheelbase must be finite and non-zero");
     return KGMT_OK;
 }
 
@@ -152,7 +162,7 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_ob
     QueryLayout L{};
     L.grid_budget = n_obstacles ? std::min<uint32_t>(kMaxGridItems, std::max<uint32_t>(8192u, 32u * std::min(n_obstacles, 4096u))) : 0u;
     const size_t T = c.tree_capacity, D = sample_dim_of(c.model);
-    const size_t R1 = (size_t)c.coarse_len * c.coarse_len * c.coarse_len;
+    const size_t R1 = regions_of(c);
     L.tiles_per_chain = (uint32_t)((T + kTileC - 1) / kTileC + 1);
     size_t cur = 0;
     L.tree = aligned(cur, T * D * 4);
@@ -209,7 +219,9 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
     volatile float cell2 = cell * cell;
     p.ws_range = range;
     p.cell_size = cell;
-    p.cell_volume = cell2 * cell;
+    p.planar = ws_dims_of(c.model) == 2 ? 1 : 0;
+    // W_R1_VOL: the coarse cell's measure in the workspace dimension
+    p.cell_volume = p.planar ? (float)cell2 : cell2 * cell;
     // a power of two divides exactly like a multiply by its reciprocal
     auto pow2 = [](float v) {
         int e = 0;
@@ -221,8 +233,8 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
     p.inv_cell = p.cell_pow2 ? 1.0f / cell : 0.0f;
     p.coarse_len = c.coarse_len;
     p.fine_len = c.fine_len;
-    p.regions = c.coarse_len * c.coarse_len * c.coarse_len;
-    p.fine_cells = c.fine_len * c.fine_len * c.fine_len;
+    p.regions = regions_of(c);
+    p.fine_cells = p.planar ? c.fine_len * c.fine_len : c.fine_len * c.fine_len * c.fine_len;
     p.v_min = c.v_min;
     p.v_max = c.v_max;
     for(int i = 0; i < 4; ++i)
@@ -231,6 +243,9 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
             volatile float span = c.u_max[i] - c.u_min[i];
             p.u_span[i] = span;
         }
+    p.pitch_min = c.pitch_min;
+    p.pitch_max = c.pitch_max;
+    p.wheelbase = c.wheelbase;
     p.nu = c.nu;
     p.mu = c.mu;
     p.gravity = c.gravity;
@@ -384,7 +399,7 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     int dev = 0, sms = 0;
     KGMT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     KGMT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-    for(int m = 1; m <= 3; ++m) grid_a_[m] = sms * propagate_blocks_per_sm((int)block, m);
+    for(int m : {1, 2, 4, 8, 15}) grid_a_[m] = sms * propagate_blocks_per_sm((int)block, m);
     grid_c_ = sms * append_blocks_per_sm();
     Sched s;
     std::memset(&s, 0, sizeof(s));
@@ -401,7 +416,7 @@ kgmt_status Engine::set_prop_block(uint32_t block)
 
 void Engine::set_models(int mask)
 {
-    mask = (mask & 3) ? (mask & 3) : 3;
+    mask = variant_of(mask & 15);
     if(mask == models_) return;
     models_ = mask;
     if(graph_)

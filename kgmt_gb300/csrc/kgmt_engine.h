@@ -58,6 +58,7 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_ob
 QueryParams make_params(const kgmt_config& c, const float* init, const float* goal, char* chunk, const QueryLayout& L, float4* obstacles,
                         uint32_t n_obstacles);
 uint32_t sample_dim_of(int32_t model);
+uint32_t ws_dims_of(int32_t model);
 kgmt_result to_result(const QueryState& s, uint64_t ticket);
 
 class Engine {
@@ -90,9 +91,16 @@ class Engine {
     kgmt_status set_prop_block(uint32_t block);
     uint32_t prop_block() const { return prop_block_; }
     // model mix of the admitted queries (bit 0 double integrator, bit 1
-    // quadrotor): picks the propagate kernel variant; a change drops the graph
+    // quadrotor, bit 2 Dubins airplane, bit 3 unicycle): picks the propagate
+    // kernel variant (single-model variants, or the one for any mix); a
+    // change drops the graph
     void set_models(int mask);
-    static int model_bit(int32_t model) { return model == KGMT_MODEL_QUADROTOR ? 2 : 1; }
+    static int model_bit(int32_t model)
+    {
+        return model == KGMT_MODEL_QUADROTOR ? 2 : model == KGMT_MODEL_DUBINS_AIRPLANE ? 4 : model == KGMT_MODEL_UNICYCLE ? 8 : 1;
+    }
+    // the propagate variant a model mask runs on
+    static int variant_of(int mask) { return (mask == 1 || mask == 2 || mask == 4 || mask == 8) ? mask : 15; }
     uint32_t iterations_launched() const { return iters_launched_; }
 
     // per-kernel CUDA-event timing (direct launches instead of the graph)
@@ -115,9 +123,9 @@ class Engine {
     uint32_t prop_block_ = 256;
     uint32_t iters_per_graph_ = 4;
     bool use_graph_ = true;
-    int grid_a_[4] = {0, 0, 0, 0};  // propagate grid per model mix
+    int grid_a_[16] = {};           // propagate grid per variant
     int grid_c_ = 0;
-    int models_ = 3;                // bit 0 double integrator, bit 1 quadrotor
+    int models_ = 15;               // propagate variant (Engine::variant_of)
     QueryParams* d_params_ = nullptr;
     QueryState* d_states_ = nullptr;
     Sched* d_sched_ = nullptr;

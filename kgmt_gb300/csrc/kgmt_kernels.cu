@@ -29,6 +29,7 @@
 // which is the order the reference's scan over node indices produces.
 #include <cstdint>
 #include <climits>
+#include <type_traits>
 
 #include "kgmt_device.cuh"
 #include "kgmt_kernels.h"
@@ -343,7 +344,7 @@ __global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32
         {
             p.parent[0] = -1;
             p.cost[0] = 0.0f;
-            p.node_r1[0] = region_of(p, p.init[0], p.init[1], p.init[2]);
+            p.node_r1[0] = region_of(p, p.init);
             QueryState st = {};
             st.status = KGMT_QUERY_RUNNING;
             st.itr = 1;
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restric
                 }
             const int x0 = grid_cell(p, fminf(a.x, b.x)), x1 = grid_cell(p, fmaxf(a.x, b.x));
             const int y0 = grid_cell(p, fminf(a.y, b.y)), y1 = grid_cell(p, fmaxf(a.y, b.y));
-            const int z0 = grid_cell(p, fminf(a.z, b.z)), z1 = grid_cell(p, fmaxf(a.z, b.z));
+            const int z0 = p.planar ? 0 : grid_cell(p, fminf(a.z, b.z)), z1 = p.planar ? 0 : grid_cell(p, fmaxf(a.z, b.z));
             for(int cx = x0; cx <= x1; ++cx)
                 for(int cy = y0; cy <= y1; ++cy)
                     for(int cz = z0; cz <= z1; ++cz) atomicAdd(&cnt[(cx * G + cy) * G + cz], 1u);
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restric
             const float4 a = p.obstacles[2 * o], b = p.obstacles[2 * o + 1];
             const int x0 = grid_cell(p, fminf(a.x, b.x)), x1 = grid_cell(p, fmaxf(a.x, b.x));
             const int y0 = grid_cell(p, fminf(a.y, b.y)), y1 = grid_cell(p, fmaxf(a.y, b.y));
-            const int z0 = grid_cell(p, fminf(a.z, b.z)), z1 = grid_cell(p, fmaxf(a.z, b.z));
+            const int z0 = p.planar ? 0 : grid_cell(p, fminf(a.z, b.z)), z1 = p.planar ? 0 : grid_cell(p, fmaxf(a.z, b.z));
             for(int cx = x0; cx <= x1; ++cx)
                 for(int cy = y0; cy <= y1; ++cy)
                     for(int cz = z0; cz <= z1; ++cz)
@@ -459,11 +460,41 @@ struct PropShared {
 };
 
 // sample rows of a model
+// SAMPLE_DIM and the number of control draws (the step draw follows them,
+// then the accept draw)
 template <int MODEL>
 struct ModelDims {
-    static constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : 10;
+    static constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : MODEL == KGMT_MODEL_UNICYCLE ? 7 : 10;
     static constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
 };
+
+// model bits of the MODELS mask a propagate variant is compiled for
+constexpr int kBitDI = 1, kBitQuad = 2, kBitDubins = 4, kBitUnicycle = 8, kAllModels = 15;
+
+// calls f(std::integral_constant<int, model>) for the query's model, among
+// the models the variant was compiled for (a single-model variant needs no test)
+template <int MODELS, typename F>
+__device__ __forceinline__ void with_model(int model, F&& f)
+{
+    if constexpr((MODELS & kBitDI) != 0)
+        if(MODELS == kBitDI || model == KGMT_MODEL_DOUBLE_INTEGRATOR) f(std::integral_constant<int, KGMT_MODEL_DOUBLE_INTEGRATOR>{});
+    if constexpr((MODELS & kBitQuad) != 0)
+        if(MODELS == kBitQuad || model == KGMT_MODEL_QUADROTOR) f(std::integral_constant<int, KGMT_MODEL_QUADROTOR>{});
+    if constexpr((MODELS & kBitDubins) != 0)
+        if(MODELS == kBitDubins || model == KGMT_MODEL_DUBINS_AIRPLANE) f(std::integral_constant<int, KGMT_MODEL_DUBINS_AIRPLANE>{});
+    if constexpr((MODELS & kBitUnicycle) != 0)
+        if(MODELS == kBitUnicycle || model == KGMT_MODEL_UNICYCLE) f(std::integral_constant<int, KGMT_MODEL_UNICYCLE>{});
+}
+
+template <int MODEL>
+__device__ __forceinline__ bool propagate_model(const QueryParams& p, const GridView& grid, const float* x0, const float* u, const float4* obs,
+                                                uint32_t n_obs, float* x1, PropCount& cnt)
+{
+    if constexpr(MODEL == KGMT_MODEL_QUADROTOR) return propagate_quad(p, grid, x0, u, obs, n_obs, x1, cnt);
+    else if constexpr(MODEL == KGMT_MODEL_DUBINS_AIRPLANE) return propagate_dubins(p, grid, x0, u, obs, n_obs, x1, cnt);
+    else if constexpr(MODEL == KGMT_MODEL_UNICYCLE) return propagate_unicycle(p, grid, x0, u, obs, n_obs, x1, cnt);
+    else return propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
+}
 
 // RK4 steps sample s will take (its step uniform alone), for ordering the
 // samples of a tile so that a warp's lanes loop about equally long
@@ -471,7 +502,7 @@ template <int MODEL>
 __device__ __forceinline__ int sample_steps(const QueryParams& p, const PropCtx& c, uint32_t s)
 {
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-    if constexpr(MODEL == KGMT_MODEL_QUADROTOR)
+    if constexpr(ModelDims<MODEL>::NC == 4)
         {
             const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
             return draw_steps(p, u01(b.x));
@@ -516,9 +547,8 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
     if(live)
         {
             float x1[D];
-            if constexpr(MODEL == KGMT_MODEL_QUADROTOR) ok = propagate_quad(p, grid, x0, u, obs, n_obs, x1, cnt);
-            else ok = propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
-            const CellIds cid = cell_ids(p, x1[0], x1[1], x1[2]);
+            ok = propagate_model<MODEL>(p, grid, x0, u, obs, n_obs, x1, cnt);
+            const CellIds cid = cell_ids(p, x1);
             r1 = cid.r1;
             bit = 1ull << cid.r2;
             float* dst = p.us + (size_t)s * D;
@@ -643,7 +673,7 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
 // launch picks the variant for the admitted mix, so a single-model batch
 // pays for one model's registers only
 template <int NT, int MODELS>
-__global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+__global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
 {
     // dynamic shared memory: boxes | grid starts | grid items | grid meta
@@ -735,7 +765,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                     cur_q = q;
                 }
             const uint32_t lt = t - bases.base[q];
-            const bool quad = (MODELS & 2) && ((MODELS & 1) == 0 || s_p.model == KGMT_MODEL_QUADROTOR);
+            const int model = s_p.model;
             // counting sort of the tile's samples by step count (dead lanes
             // last): thread i then takes the i-th sample in that order
             {
@@ -744,14 +774,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                 if(s0 < s_c.n_samples)
                     {
                         int k = 1;
-                        if constexpr((MODELS & 2) != 0)
-                            {
-                                if(quad) k = sample_steps<KGMT_MODEL_QUADROTOR>(s_p, s_c, s0);
-                            }
-                        if constexpr((MODELS & 1) != 0)
-                            {
-                                if(!quad) k = sample_steps<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, s0);
-                            }
+                        with_model<MODELS>(model, [&](auto m) { k = sample_steps<decltype(m)::value>(s_p, s_c, s0); });
                         key = k < kSortBins - 1 ? k : kSortBins - 2;
                     }
                 if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = 0;
@@ -782,14 +805,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
             uint32_t par = 0;
             if(live)
                 {
-                    if constexpr((MODELS & 2) != 0)
-                        {
-                            if(quad) par = prepare_sample<KGMT_MODEL_QUADROTOR>(s_p, s_c, s, x0, u);
-                        }
-                    if constexpr((MODELS & 1) != 0)
-                        {
-                            if(!quad) par = prepare_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, s_c, s, x0, u);
-                        }
+                    with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(s_p, s_c, s, x0, u); });
                 }
             if(wait_obs)
                 {
@@ -803,14 +819,7 @@ __global__ void __launch_bounds__(NT, (MODELS == 1 ? 1024 : 512) / NT) k_propaga
                     phase ^= 1u;
                 }
             const GridView grid{(s_p.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, s_p.grid_items};
-            if constexpr((MODELS & 2) != 0)
-                {
-                    if(quad) finish_sample<KGMT_MODEL_QUADROTOR>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
-                }
-            if constexpr((MODELS & 1) != 0)
-                {
-                    if(!quad) finish_sample<KGMT_MODEL_DOUBLE_INTEGRATOR>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh);
-                }
+            with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh); });
             __syncthreads();
             if(threadIdx.x == 0)
                 {
@@ -999,7 +1008,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                             float* dst = p.tree + (size_t)idx * D;
                             for(int c = 0; c < D; ++c) dst[c] = src[c];
                             p.parent[idx] = p.up[s];
-                            const float dist = goal_distance(src[0], src[1], src[2], p);
+                            const float dist = goal_distance(p, src);
                             p.cost[idx] = dist;
                             p.node_r1[idx] = p.ur1[s];
                             for(uint32_t r = 0; r < w[j]; ++r, ++iw)
@@ -1077,13 +1086,27 @@ __global__ void k_paths(const QueryParams* __restrict__ P, QueryState* S, uint32
 // ---------------------------------------------------------------------------
 // obstacles: [n][6] rows (min xyz, max xyz) -> [n][2] float4 in the arena
 // ---------------------------------------------------------------------------
-__global__ void k_stage_obstacles(const float* __restrict__ src, float4* dst, uint32_t n)
+// rows of 2W floats (min corner, max corner; W = 3, or 2 for the planar
+// model, whose z extents are then 0 and never tested) -> float4 pairs
+__device__ __forceinline__ void stage_box(const float* r, int w, float4* dst)
+{
+    if(w == 2)
+        {
+            dst[0] = make_float4(r[0], r[1], 0.0f, 0.0f);
+            dst[1] = make_float4(r[2], r[3], 0.0f, 0.0f);
+        }
+    else
+        {
+            dst[0] = make_float4(r[0], r[1], r[2], 0.0f);
+            dst[1] = make_float4(r[3], r[4], r[5], 0.0f);
+        }
+}
+
+__global__ void k_stage_obstacles(const float* __restrict__ src, float4* dst, uint32_t n, int w)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= n) return;
-    const float* r = src + (size_t)i * 6;
-    dst[2 * i] = make_float4(r[0], r[1], r[2], 0.0f);
-    dst[2 * i + 1] = make_float4(r[3], r[4], r[5], 0.0f);
+    stage_box(src + (size_t)i * 2 * w, w, dst + 2 * i);
 }
 
 // ---------------------------------------------------------------------------
@@ -1094,12 +1117,8 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
                                     int32_t* r1, int32_t* r2)
 {
     extern __shared__ float4 s_obs[];
-    for(uint32_t i = threadIdx.x; i < n_obs; i += blockDim.x)
-        {
-            const float* r = obs_rows + (size_t)i * 6;
-            s_obs[2 * i] = make_float4(r[0], r[1], r[2], 0.0f);
-            s_obs[2 * i + 1] = make_float4(r[3], r[4], r[5], 0.0f);
-        }
+    const int w = p.planar ? 2 : 3;
+    for(uint32_t i = threadIdx.x; i < n_obs; i += blockDim.x) stage_box(obs_rows + (size_t)i * 2 * w, w, s_obs + 2 * i);
     __syncthreads();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if(s >= n) return;
@@ -1109,11 +1128,11 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
     for(int j = 0; j < 8; ++j) u[j] = uni[(size_t)s * 8 + j];
     PropCount cnt;
     const GridView none{nullptr, nullptr, nullptr};
-    bool ok = p.model == KGMT_MODEL_QUADROTOR ? propagate_quad(p, none, a, u, s_obs, n_obs, b, cnt)
-                                              : propagate_di(p, none, a, u, s_obs, n_obs, b, cnt);
+    bool ok = false;
+    with_model<kAllModels>(p.model, [&](auto m) { ok = propagate_model<decltype(m)::value>(p, none, a, u, s_obs, n_obs, b, cnt); });
     for(int j = 0; j < D; ++j) x1[(size_t)s * D + j] = b[j];
     valid[s] = ok ? 1 : 0;
-    const CellIds c = cell_ids(p, b[0], b[1], b[2]);
+    const CellIds c = cell_ids(p, b);
     if(r1) r1[s] = c.r1;
     if(r2) r2[s] = c.r2;
 }
@@ -1133,9 +1152,11 @@ static cudaError_t launch_propagate_m(const LaunchArgs& a, int models, int grid,
 {
     switch(models)
         {
-            case 1: return launch_propagate_t<NT, 1>(a, grid, s);
-            case 2: return launch_propagate_t<NT, 2>(a, grid, s);
-            default: return launch_propagate_t<NT, 3>(a, grid, s);
+            case kBitDI: return launch_propagate_t<NT, kBitDI>(a, grid, s);
+            case kBitQuad: return launch_propagate_t<NT, kBitQuad>(a, grid, s);
+            case kBitDubins: return launch_propagate_t<NT, kBitDubins>(a, grid, s);
+            case kBitUnicycle: return launch_propagate_t<NT, kBitUnicycle>(a, grid, s);
+            default: return launch_propagate_t<NT, kAllModels>(a, grid, s);
         }
 }
 
@@ -1156,9 +1177,11 @@ static int occupancy_m(int models)
     const size_t smem = kPropSmemBytes;
     switch(models)
         {
-            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 1>, NT, smem); break;
-            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 2>, NT, smem); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, 3>, NT, smem); break;
+            case kBitDI: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitDI>, NT, smem); break;
+            case kBitQuad: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitQuad>, NT, smem); break;
+            case kBitDubins: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitDubins>, NT, smem); break;
+            case kBitUnicycle: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitUnicycle>, NT, smem); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kAllModels>, NT, smem); break;
         }
     return n;
 }
@@ -1211,10 +1234,10 @@ cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, cudaStream_t s)
+cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, int ws_dims, cudaStream_t s)
 {
     if(n == 0) return cudaSuccess;
-    k_stage_obstacles<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n);
+    k_stage_obstacles<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n, ws_dims == 2 ? 2 : 3);
     return cudaGetLastError();
 }
 

@@ -122,7 +122,7 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
     int dev = 0, sms = 0;
     NA_CHECK(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
     NA_CHECK(cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
-    const int models = Engine::model_bit(cfg->model);
+    const int models = Engine::variant_of(Engine::model_bit(cfg->model));
     const int grid_a = sms * propagate_blocks_per_sm((int)block, models);
     const int grid_c = sms * append_blocks_per_sm();
 
@@ -138,7 +138,7 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
     NA_CHECK(cuda_status(cudaMemsetAsync(d_tiles, 0, 5 * sizeof(uint32_t), s), "memset(tiles)"));
     // params and sched live on this host stack frame: finish the copies first
     NA_CHECK(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
-    NA_CHECK(cuda_status(launch_stage_obstacles(d_obstacles, params.obstacles, n_obstacles, s), "stage obstacles"));
+    NA_CHECK(cuda_status(launch_stage_obstacles(d_obstacles, params.obstacles, n_obstacles, (int)ws_dims_of(cfg->model), s), "stage obstacles"));
     NA_CHECK(cuda_status(launch_admit(a, 0, 1, s), "k_admit"));
     NA_CHECK(cuda_status(launch_schedule(a, s), "k_schedule"));
 

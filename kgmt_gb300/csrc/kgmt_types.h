@@ -32,6 +32,18 @@ constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-a
 // made of: 4 ode evaluations of ~139, stage and update combinations, checks)
 constexpr uint32_t kOpsPerStepDI = 81;
 constexpr uint32_t kOpsPerStepQuad = 658;
+// Dubins airplane: 4 portable sine/cosine pairs (~26 each: reduction, two
+// polynomials, quadrant selection), 4 attitude offsets, 12 stage products,
+// 23 for the three position sums, 3 updates, 10 compares
+constexpr uint32_t kOpsPerStepDubins = 148;
+// unicycle: one sine/cosine pair, 14 for the Euler update, 4 compares
+constexpr uint32_t kOpsPerStepUnicycle = 44;
+__host__ __device__ constexpr uint32_t ops_per_step(int32_t model)
+{
+    return model == KGMT_MODEL_QUADROTOR ? kOpsPerStepQuad
+         : model == KGMT_MODEL_DUBINS_AIRPLANE ? kOpsPerStepDubins
+         : model == KGMT_MODEL_UNICYCLE ? kOpsPerStepUnicycle : kOpsPerStepDI;
+}
 constexpr uint32_t kOpsPerObstacleTest = 6;
 constexpr uint32_t kOpsPerGridLookup = 24;  // six cell coordinates of the step box
 
@@ -69,6 +81,9 @@ struct QueryParams {
     uint32_t coarse_len, fine_len, regions, fine_cells;
     float v_min, v_max;
     float u_min[4], u_span[4];
+    int32_t planar;                // 1: 2-D workspace (unicycle), z of every position = ws_min
+    float pitch_min, pitch_max;    // Dubins airplane
+    float wheelbase;               // unicycle
     float nu, mu, gravity, mass_inv;
     float iix, iiy, iiz;  // 1 / I
     float jx, jy, jz;     // (Iy - Iz) / Ix, (Iz - Ix) / Iy, (Ix - Iy) / Iz

@@ -5,6 +5,8 @@
     python -m kgmt_gb300.measure batch      # 3: 256 double-integrator queries, batched
     python -m kgmt_gb300.measure mixed      # 4: 1024 mixed queries, batched, checked against plain
     python -m kgmt_gb300.measure served     # 5: Poisson stream from the mixed set, continuous batching
+    python -m kgmt_gb300.measure dubins     # Dubins airplane: plain single queries, then 256 batched
+    python -m kgmt_gb300.measure unicycle   # planar unicycle: plain single queries, then 256 batched
 
 Queries/s, p50/p99 solve latency, success rate; the plain form (one query per
 launch chain) is measured beside the batched and served forms on the same
@@ -28,8 +30,9 @@ def _pct(x, p):
 
 
 def _device_obstacles(q):
+    # the single-query plan takes the model's own rows (4 floats for the planar unicycle)
     import torch
-    return torch.from_numpy(np.ascontiguousarray(q.obstacles, np.float32).reshape(-1, 6)).to("cuda")
+    return torch.from_numpy(np.ascontiguousarray(W.boxes_for_plan(q), np.float32)).to("cuda")
 
 
 def plain_run(queries, repeat: int = 1):
@@ -68,6 +71,28 @@ def m_single(args):
     times, res = plain_run(qs, repeat=1)
     times2, _ = plain_run(qs, repeat=1)  # warm second pass
     return summarise("single double integrator, T=100k, 10 boxes, plain", times2, res)
+
+
+def _model_workload(name, make, args):
+    """Plain single queries of one model, then 256 of them batched."""
+    qs = [make(seed=s) for s in range(1, args.n + 1)]
+    plain_run(qs[:1])
+    times, res = plain_run(qs)
+    line = summarise(name + ", plain", times, res)
+    batch = [make(seed=1000 + s) for s in range(256)]
+    walls, bres, _ = _batched(batch, args.reps)
+    wall = float(np.median(walls))
+    line.update({"batched_256_queries_per_s": len(batch) / wall, "batched_ms": wall * 1e3,
+                 "batched_success_rate": float(np.mean([r["status"] == 1 for r in bres]))})
+    return line
+
+
+def m_dubins(args):
+    return _model_workload("Dubins airplane, T=200k, 10 boxes", W.dubins_query, args)
+
+
+def m_unicycle(args):
+    return _model_workload("planar unicycle, T=100k, 10 boxes", W.unicycle_query, args)
 
 
 def m_quad(args):
@@ -168,7 +193,7 @@ def m_served(args):
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["single", "quad", "batch", "mixed", "served"])
+    ap.add_argument("what", choices=["single", "quad", "batch", "mixed", "served", "dubins", "unicycle"])
     ap.add_argument("--n", type=int, default=16, help="queries for the plain single-query workloads")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--n-mixed", type=int, default=1024)
@@ -179,7 +204,8 @@ def main(argv=None) -> int:
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--iters-per-step", type=int, default=2)
     a = ap.parse_args(argv)
-    fn = {"single": m_single, "quad": m_quad, "batch": m_batch, "mixed": m_mixed, "served": m_served}[a.what]
+    fn = {"single": m_single, "quad": m_quad, "batch": m_batch, "mixed": m_mixed, "served": m_served, "dubins": m_dubins,
+          "unicycle": m_unicycle}[a.what]
     out = fn(a)
     for line in out if isinstance(out, list) else [out]:
         print(json.dumps(line), flush=True)

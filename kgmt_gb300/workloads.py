@@ -15,7 +15,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .config import (MAX_SAMPLE_DIM, MODEL_DOUBLE_INTEGRATOR, MODEL_QUADROTOR, PlannerConfig,
-                     double_integrator_batched, double_integrator_single, quadrotor_large, sample_dim)
+                     double_integrator_batched, double_integrator_single, dubins_airplane, quadrotor_large, sample_dim,
+                     unicycle)
 
 
 @dataclass
@@ -77,6 +78,82 @@ def quadrotor_query(seed: int = 1, n_obstacles: int = 200, **overrides) -> Query
     goal = np.float32([0.95, 0.95, 0.95])
     obs = random_boxes(_rng(seed * 7919 + 13), n_obstacles, 0.02, 0.1, start, goal, cfg.goal_radius)
     return Query(cfg, _state(cfg.model, start), _state(cfg.model, goal), obs)
+
+
+def dubins_query(seed: int = 1, n_obstacles: int = 10, **overrides) -> Query:
+    """Single Dubins-airplane query: 10 boxes with edges U[0.05, 0.15], start
+    (0.05, 0.05, 0.05) heading yaw pi/4, pitch 0.4, speed 0.15; goal ball
+    r=0.05 at (0.95, 0.95, 0.95)."""
+    cfg = dubins_airplane(seed).replace(**overrides)
+    start = np.float32([0.05, 0.05, 0.05])
+    goal = np.float32([0.95, 0.95, 0.95])
+    obs = random_boxes(_rng(seed * 7919 + 17), n_obstacles, 0.05, 0.15, start, goal, cfg.goal_radius)
+    init = np.zeros(cfg.sample_dim, np.float32)
+    init[:6] = [start[0], start[1], start[2], math.pi / 4, 0.4, 0.15]
+    return Query(cfg, init, _state(cfg.model, goal), obs)
+
+
+def planar_boxes(rng: np.random.Generator, n: int, edge_lo: float, edge_hi: float, start: np.ndarray, goal: np.ndarray,
+                 goal_r: float, margin: float = 0.01) -> np.ndarray:
+    """n boxes in the plane, centres U[0.1, 0.9]^2, edges U[edge_lo, edge_hi],
+    stored as rows of 6 with z extents [0, 1] (a planar query ignores them)."""
+    out = np.zeros((n, 6), np.float32)
+    i = 0
+    while i < n:
+        c = rng.uniform(0.1, 0.9, 2)
+        e = rng.uniform(edge_lo, edge_hi, 2)
+        lo, hi = c - e / 2, c + e / 2
+        if np.all(start >= lo - margin) and np.all(start <= hi + margin):
+            continue
+        if float(np.linalg.norm(np.clip(goal, lo, hi) - goal)) <= goal_r + margin:
+            continue
+        out[i] = [lo[0], lo[1], 0.0, hi[0], hi[1], 1.0]
+        i += 1
+    return out
+
+
+def unicycle_query(seed: int = 1, n_obstacles: int = 10, **overrides) -> Query:
+    """Single planar unicycle query: 10 boxes with edges U[0.05, 0.15], start
+    (0.05, 0.05) heading pi/4 at speed 0.1; goal disc r=0.05 at (0.95, 0.95)."""
+    cfg = unicycle(seed).replace(**overrides)
+    start = np.float32([0.05, 0.05])
+    goal = np.float32([0.95, 0.95])
+    obs = planar_boxes(_rng(seed * 7919 + 19), n_obstacles, 0.05, 0.15, start, goal, cfg.goal_radius)
+    init = np.zeros(cfg.sample_dim, np.float32)
+    init[:4] = [start[0], start[1], math.pi / 4, 0.1]
+    goal_row = np.zeros(cfg.sample_dim, np.float32)
+    goal_row[:2] = goal
+    return Query(cfg, init, goal_row, obs)
+
+
+def boxes_for_plan(q: Query) -> np.ndarray:
+    """The query's boxes in its model's own layout: rows of 4 (x, y extents)
+    for the planar unicycle, rows of 6 otherwise -- what the single-query
+    plan takes, like the reference's [n][2 * W_DIM] array."""
+    if q.config.ws_dims == 2:
+        return np.ascontiguousarray(q.obstacles[:, [0, 1, 3, 4]])
+    return q.obstacles
+
+
+def all_models_batch(n_queries: int = 64, seed: int = 1, tree_capacity: int = 20_000) -> list[Query]:
+    """Heterogeneous batch cycling through the four models (unicycle, double
+    integrator, Dubins airplane, quadrotor), each query with its own seed and
+    scene."""
+    out = []
+    for q in range(n_queries):
+        s = seed * 1_000_003 + q
+        m = q % 4
+        if m == 0:
+            out.append(unicycle_query(seed=s, tree_capacity=tree_capacity))
+        elif m == 1:
+            qq = double_integrator_query(seed=s)
+            qq.config = qq.config.replace(tree_capacity=tree_capacity)
+            out.append(qq)
+        elif m == 2:
+            out.append(dubins_query(seed=s, tree_capacity=tree_capacity))
+        else:
+            out.append(quadrotor_query(seed=s, n_obstacles=50, tree_capacity=tree_capacity, coarse_len=8, fine_len=2))
+    return out
 
 
 def double_integrator_batch(n_queries: int = 256, n_obstacles: int = 50, seed: int = 1, **overrides) -> list[Query]:

@@ -172,8 +172,10 @@ long ko_check_div6(void)
     return bad;
 }
 
-int ko_sample_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 17 : 10; }
-int ko_state_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 12 : 6; }
+/* SAMPLE_DIM / STATE_DIM per model (statePropagator.cu rows x1[...]) */
+int ko_sample_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 17 : model == KO_MODEL_UNICYCLE ? 7 : 10; }
+int ko_state_dim(int32_t model) { return model == KO_MODEL_QUADROTOR ? 12 : model == KO_MODEL_UNICYCLE ? 4 : 6; }
+int ko_ws_dims(int32_t model) { return model == KO_MODEL_UNICYCLE ? 2 : 3; }
 
 /* ------------------------------------------------------------------------ */
 /* Regions (workspace-only grids).  Graph.cu:99-153 (getRegion: z least     */
@@ -187,11 +189,14 @@ static inline int cell_index(float t, int len)
     return i > len - 1 ? len - 1 : i;
 }
 
+/* W workspace digits, x most significant: r1 = ix*L + iy (W = 2) or
+ * (ix*L + iy)*L + iz (W = 3), Graph.cu:105-113 */
 static void coarse_idx(const ko_config* c, const float* x, int idx[3])
 {
     float range = c->ws_max - c->ws_min;
     float L = (float)c->coarse_len;
-    for(int d = 0; d < 3; ++d)
+    int w = ko_ws_dims(c->model);
+    for(int d = 0; d < w; ++d)
         {
             float t = (L * (x[d] - c->ws_min)) / range;
             idx[d] = cell_index(t, (int)c->coarse_len);
@@ -203,51 +208,65 @@ int ko_region(const ko_config* c, const float* x)
     int idx[3];
     coarse_idx(c, x, idx);
     int L = (int)c->coarse_len;
+    if(ko_ws_dims(c->model) == 2) return idx[0] * L + idx[1];
     return (idx[0] * L + idx[1]) * L + idx[2];
 }
 
 int ko_subregion(const ko_config* c, const float* x, int r1)
 {
     int L = (int)c->coarse_len;
-    int idx[3] = {r1 / (L * L), (r1 / L) % L, r1 % L};
+    int w = ko_ws_dims(c->model);
+    int idx[3];
+    if(w == 2) idx[0] = r1 / L, idx[1] = r1 % L;
+    else idx[0] = r1 / (L * L), idx[1] = (r1 / L) % L, idx[2] = r1 % L;
     float size1 = (c->ws_max - c->ws_min) / (float)c->coarse_len;
     float L2 = (float)c->fine_len;
     int j[3];
-    for(int d = 0; d < 3; ++d)
+    for(int d = 0; d < w; ++d)
         {
             float minr = c->ws_min + (float)idx[d] * size1;
             float t = (L2 * (x[d] - minr)) / size1;
             j[d] = cell_index(t, (int)c->fine_len);
         }
     int F = (int)c->fine_len;
+    if(w == 2) return j[0] * F + j[1];
     return (j[0] * F + j[1]) * F + j[2];
 }
 
-float ko_distance(const float* a, const float* b)
+/* helper.cuh:138-152 over the first w components */
+float ko_distance_w(const float* a, const float* b, int w)
 {
-    float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
-    float s = (dx * dx + dy * dy) + dz * dz;
+    float dx = a[0] - b[0], dy = a[1] - b[1];
+    float s = dx * dx + dy * dy;
+    if(w == 3)
+        {
+            float dz = a[2] - b[2];
+            s = s + dz * dz;
+        }
     return sqrtf(s);
 }
+
+float ko_distance(const float* a, const float* b) { return ko_distance_w(a, b, 3); }
 
 /* ------------------------------------------------------------------------ */
 /* Collision: collisionCheck.cu:3-10 (separated iff bbMax <= obsMin or      */
 /* obsMax <= bbMin on some axis; touching counts as free) and 49-61.        */
 /* ------------------------------------------------------------------------ */
-static int motion_valid_f(const float* p0, const float* p1, const float* obs, uint32_t n_obs)
+/* w: workspace dimension; boxes are rows of 2w floats */
+static int motion_valid_f(const float* p0, const float* p1, const float* obs, uint32_t n_obs, int w)
 {
     float bmin[3], bmax[3];
-    for(int d = 0; d < 3; ++d)
+    for(int d = 0; d < w; ++d)
         {
             if(p0[d] > p1[d]) bmin[d] = p1[d], bmax[d] = p0[d];
             else bmin[d] = p0[d], bmax[d] = p1[d];
         }
     for(uint32_t o = 0; o < n_obs; ++o)
         {
-            const float* b = obs + 6 * (size_t)o;
+            const float* b = obs + 2 * w * (size_t)o;
             int sep = 0;
-            for(int d = 0; d < 3; ++d)
-                if(bmax[d] <= b[d] || b[3 + d] <= bmin[d]) sep = 1;
+            for(int d = 0; d < w; ++d)
+                if(bmax[d] <= b[d] || b[w + d] <= bmin[d]) sep = 1;
             if(!sep) return 0;
         }
     return 1;
@@ -255,23 +274,23 @@ static int motion_valid_f(const float* p0, const float* p1, const float* obs, ui
 
 int ko_segment_valid(const float* p0, const float* p1, const float* obstacles, uint32_t n_obs)
 {
-    return motion_valid_f(p0, p1, obstacles, n_obs);
+    return motion_valid_f(p0, p1, obstacles, n_obs, 3);
 }
 
-static int motion_valid_d(const double* p0, const double* p1, const float* obs, uint32_t n_obs)
+static int motion_valid_d(const double* p0, const double* p1, const float* obs, uint32_t n_obs, int w)
 {
     double bmin[3], bmax[3];
-    for(int d = 0; d < 3; ++d)
+    for(int d = 0; d < w; ++d)
         {
             if(p0[d] > p1[d]) bmin[d] = p1[d], bmax[d] = p0[d];
             else bmin[d] = p0[d], bmax[d] = p1[d];
         }
     for(uint32_t o = 0; o < n_obs; ++o)
         {
-            const float* b = obs + 6 * (size_t)o;
+            const float* b = obs + 2 * w * (size_t)o;
             int sep = 0;
-            for(int d = 0; d < 3; ++d)
-                if(bmax[d] <= (double)b[d] || (double)b[3 + d] <= bmin[d]) sep = 1;
+            for(int d = 0; d < w; ++d)
+                if(bmax[d] <= (double)b[d] || (double)b[w + d] <= bmin[d]) sep = 1;
             if(!sep) return 0;
         }
     return 1;
@@ -290,10 +309,17 @@ static double bound_margin_d(const ko_config* c, const double* pos, const double
     return m;
 }
 
-static double face_margin_d(const double* p0, const double* p1, const float* obs, uint32_t n_obs)
+/* distance of a value to a closed interval's two ends */
+static double end_margin_d(double x, double lo, double hi)
+{
+    double a = fabs(x - lo), b = fabs(x - hi);
+    return a < b ? a : b;
+}
+
+static double face_margin_d(const double* p0, const double* p1, const float* obs, uint32_t n_obs, int w)
 {
     double bmin[3], bmax[3], m = 1e30;
-    for(int d = 0; d < 3; ++d)
+    for(int d = 0; d < w; ++d)
         {
             if(p0[d] > p1[d]) bmin[d] = p1[d], bmax[d] = p0[d];
             else bmin[d] = p0[d], bmax[d] = p1[d];
@@ -303,12 +329,12 @@ static double face_margin_d(const double* p0, const double* p1, const float* obs
      * only when it crosses zero */
     for(uint32_t o = 0; o < n_obs; ++o)
         {
-            const float* b = obs + 6 * (size_t)o;
+            const float* b = obs + 2 * w * (size_t)o;
             double sep = -1e30;
-            for(int d = 0; d < 3; ++d)
+            for(int d = 0; d < w; ++d)
                 {
                     double a1 = (double)b[d] - bmax[d];
-                    double a2 = bmin[d] - (double)b[3 + d];
+                    double a2 = bmin[d] - (double)b[w + d];
                     double s = a1 > a2 ? a1 : a2;
                     if(s > sep) sep = s;
                 }
@@ -367,7 +393,7 @@ static int prop_di_f(const ko_config* c, const float* x0, const float* u, const 
                     ok = 0;
                     break;
                 }
-            if(!motion_valid_f(p0, p, obs, n_obs))
+            if(!motion_valid_f(p0, p, obs, n_obs, 3))
                 {
                     ok = 0;
                     break;
@@ -416,9 +442,9 @@ static int prop_di_d(const ko_config* c, const float* x0, const float* u, const 
                     ok = 0;
                     break;
                 }
-            double fm = face_margin_d(p0, p, obs, n_obs);
+            double fm = face_margin_d(p0, p, obs, n_obs, 3);
             if(fm < m) m = fm;
-            if(!motion_valid_d(p0, p, obs, n_obs))
+            if(!motion_valid_d(p0, p, obs, n_obs, 3))
                 {
                     ok = 0;
                     break;
@@ -502,7 +528,7 @@ static int prop_quad_f(const ko_config* c, const float* x0, const float* u, cons
                     ok = 0;
                     break;
                 }
-            if(!motion_valid_f(p0, s, obs, n_obs))
+            if(!motion_valid_f(p0, s, obs, n_obs, 3))
                 {
                     ok = 0;
                     break;
@@ -573,9 +599,9 @@ static int prop_quad_d(const ko_config* c, const float* x0, const float* u, cons
                     ok = 0;
                     break;
                 }
-            double fm = face_margin_d(p0, s, obs, n_obs);
+            double fm = face_margin_d(p0, s, obs, n_obs, 3);
             if(fm < m) m = fm;
-            if(!motion_valid_d(p0, s, obs, n_obs))
+            if(!motion_valid_d(p0, s, obs, n_obs, 3))
                 {
                     ok = 0;
                     break;
@@ -588,10 +614,229 @@ static int prop_quad_d(const ko_config* c, const float* x0, const float* u, cons
     return ok;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Dubins airplane (statePropagator.cu:147-244).  State x y z yaw pitch v;   */
+/* draws a, yaw rate, pitch rate, steps; row [state | yr pr a | k*h].  The   */
+/* attitude is linear in time within a step, so the RK4 stages are the       */
+/* closed forms at t, t + h/2, t + h, summed in the reference's order        */
+/* (v cos p) cos y + 2 (A + A) + B, weighted by h/6.  Checks: speed, pitch,  */
+/* workspace, obstacles.  FP32 mirror: the end-stage attitude sine/cosine is */
+/* the next step's start pair, exactly as the CUDA kernel carries it.        */
+/* ------------------------------------------------------------------------ */
+static int prop_dubins_f(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, float* x1)
+{
+    float ctrl[3];
+    int k;
+    draw_controls(c, u, ctrl, &k);
+    const float a = ctrl[0], yr = ctrl[1], pr = ctrl[2];
+    const float h = c->step_size, hh = 0.5f * h, h6 = h / 6.0f;
+    float x = x0[0], y = x0[1], z = x0[2], yaw = x0[3], pitch = x0[4], v = x0[5];
+    const float dvm = hh * a, dve = h * a;
+    const float dpm = hh * pr, dym = hh * yr;
+    const float dpe = h * pr, dye = h * yr;
+    const float dv = h6 * ((a + 2.0f * (a + a)) + a);
+    float sp, cp, sy, cy;
+    ko_sincosf(pitch, &sp, &cp);
+    ko_sincosf(yaw, &sy, &cy);
+    int ok = 1;
+    for(int i = 0; i < k; ++i)
+        {
+            float p0[3] = {x, y, z};
+            float spm, cpm, sym, cym, spe, cpe, sye, cye;
+            ko_sincosf(pitch + dpm, &spm, &cpm);
+            ko_sincosf(yaw + dym, &sym, &cym);
+            ko_sincosf(pitch + dpe, &spe, &cpe);
+            ko_sincosf(yaw + dye, &sye, &cye);
+            const float vm = v + dvm, ve = v + dve;
+            const float ax = (vm * cpm) * cym, bx = (ve * cpe) * cye;
+            const float ay = (vm * cpm) * sym, by = (ve * cpe) * sye;
+            const float az = vm * spm, bz = ve * spe;
+            x = x + h6 * ((((v * cp) * cy) + 2.0f * (ax + ax)) + bx);
+            y = y + h6 * ((((v * cp) * sy) + 2.0f * (ay + ay)) + by);
+            z = z + h6 * (((v * sp) + 2.0f * (az + az)) + bz);
+            yaw = yaw + dye;
+            pitch = pitch + dpe;
+            v = v + dv;
+            sp = spe, cp = cpe, sy = sye, cy = cye;
+            if(v < c->v_min || v > c->v_max || pitch < c->pitch_min || pitch > c->pitch_max || x < c->ws_min || x > c->ws_max ||
+               y < c->ws_min || y > c->ws_max || z < c->ws_min || z > c->ws_max)
+                {
+                    ok = 0;
+                    break;
+                }
+            float p1[3] = {x, y, z};
+            if(!motion_valid_f(p0, p1, obs, n_obs, 3))
+                {
+                    ok = 0;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = z, x1[3] = yaw, x1[4] = pitch, x1[5] = v;
+    x1[6] = yr, x1[7] = pr, x1[8] = a;
+    x1[9] = h * (float)k;
+    return ok;
+}
+
+static int prop_dubins_d(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, double* x1, double* margin)
+{
+    float cf[3];
+    int k;
+    draw_controls(c, u, cf, &k);
+    const double a = cf[0], yr = cf[1], pr = cf[2];
+    const double h = (double)c->step_size;
+    double x = x0[0], y = x0[1], z = x0[2], yaw = x0[3], pitch = x0[4], v = x0[5];
+    int ok = 1;
+    double m = 1e30;
+    for(int i = 0; i < k; ++i)
+        {
+            double p0[3] = {x, y, z};
+            /* classic RK4 of x' = v cos p cos y, y' = v cos p sin y, z' = v sin p
+             * with p, y, v linear in time */
+            double pm = pitch + 0.5 * h * pr, ym = yaw + 0.5 * h * yr, pe = pitch + h * pr, ye = yaw + h * yr;
+            double vm = v + 0.5 * h * a, ve = v + h * a;
+            x += h / 6.0 * (v * cos(pitch) * cos(yaw) + 4.0 * vm * cos(pm) * cos(ym) + ve * cos(pe) * cos(ye));
+            y += h / 6.0 * (v * cos(pitch) * sin(yaw) + 4.0 * vm * cos(pm) * sin(ym) + ve * cos(pe) * sin(ye));
+            z += h / 6.0 * (v * sin(pitch) + 4.0 * vm * sin(pm) + ve * sin(pe));
+            yaw = ye;
+            pitch = pe;
+            v = ve;
+            double pos[3] = {x, y, z};
+            double bm = end_margin_d(v, c->v_min, c->v_max);
+            double t = end_margin_d(pitch, c->pitch_min, c->pitch_max);
+            if(t < bm) bm = t;
+            for(int d = 0; d < 3; ++d)
+                {
+                    t = end_margin_d(pos[d], c->ws_min, c->ws_max);
+                    if(t < bm) bm = t;
+                }
+            if(bm < m) m = bm;
+            if(v < c->v_min || v > c->v_max || pitch < c->pitch_min || pitch > c->pitch_max || x < c->ws_min || x > c->ws_max ||
+               y < c->ws_min || y > c->ws_max || z < c->ws_min || z > c->ws_max)
+                {
+                    ok = 0;
+                    break;
+                }
+            double fm = face_margin_d(p0, pos, obs, n_obs, 3);
+            if(fm < m) m = fm;
+            if(!motion_valid_d(p0, pos, obs, n_obs, 3))
+                {
+                    ok = 0;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = z, x1[3] = yaw, x1[4] = pitch, x1[5] = v;
+    x1[6] = yr, x1[7] = pr, x1[8] = a;
+    x1[9] = h * (double)k;
+    if(margin) *margin = m;
+    return ok;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Unicycle (statePropagator.cu:13-74), planar.  State x y theta v; draws a, */
+/* steering, dt, steps; row [state | a steering dt].  Explicit Euler in the  */
+/* reference's order; tan(steering), the same every step, is taken as the    */
+/* portable sin/cos ratio.  Checks: workspace (x, y), then the boxes in the  */
+/* plane; the reference has no speed check.                                  */
+/* ------------------------------------------------------------------------ */
+static int prop_uni_f(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, float* x1)
+{
+    float ctrl[3];
+    int k;
+    draw_controls(c, u, ctrl, &k);
+    const float a = ctrl[0], steer = ctrl[1], dt = ctrl[2];
+    const float h = c->step_size;
+    float x = x0[0], y = x0[1], th = x0[2], v = x0[3];
+    float ss, cs;
+    ko_sincosf(steer, &ss, &cs);
+    const float tan_steer = ss / cs;
+    int ok = 1;
+    for(int i = 0; i < k; ++i)
+        {
+            float p0[2] = {x, y};
+            float st, ct;
+            ko_sincosf(th, &st, &ct);
+            x = x + (v * ct) * h;
+            y = y + (v * st) * h;
+            th = th + ((v / c->wheelbase) * tan_steer) * h;
+            v = v + a * h;
+            if(x < c->ws_min || x > c->ws_max || y < c->ws_min || y > c->ws_max)
+                {
+                    ok = 0;
+                    break;
+                }
+            float p1[2] = {x, y};
+            if(!motion_valid_f(p0, p1, obs, n_obs, 2))
+                {
+                    ok = 0;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = th, x1[3] = v;
+    x1[4] = a, x1[5] = steer, x1[6] = dt;
+    return ok;
+}
+
+static int prop_uni_d(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, double* x1, double* margin)
+{
+    float cf[3];
+    int k;
+    draw_controls(c, u, cf, &k);
+    const double a = cf[0], steer = cf[1], dt = cf[2];
+    const double h = (double)c->step_size, tan_steer = tan(steer);
+    double x = x0[0], y = x0[1], th = x0[2], v = x0[3];
+    int ok = 1;
+    double m = 1e30;
+    for(int i = 0; i < k; ++i)
+        {
+            double p0[2] = {x, y};
+            double ct = cos(th), st = sin(th);
+            x += v * ct * h;
+            y += v * st * h;
+            th += (v / (double)c->wheelbase) * tan_steer * h;
+            v += a * h;
+            double bm = end_margin_d(x, c->ws_min, c->ws_max), t = end_margin_d(y, c->ws_min, c->ws_max);
+            if(t < bm) bm = t;
+            if(bm < m) m = bm;
+            if(x < c->ws_min || x > c->ws_max || y < c->ws_min || y > c->ws_max)
+                {
+                    ok = 0;
+                    break;
+                }
+            double p1[2] = {x, y};
+            double fm = face_margin_d(p0, p1, obs, n_obs, 2);
+            if(fm < m) m = fm;
+            if(!motion_valid_d(p0, p1, obs, n_obs, 2))
+                {
+                    ok = 0;
+                    break;
+                }
+        }
+    x1[0] = x, x1[1] = y, x1[2] = th, x1[3] = v;
+    x1[4] = a, x1[5] = steer, x1[6] = dt;
+    if(margin) *margin = m;
+    return ok;
+}
+
 static int propagate_one_f(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, float* x1)
 {
-    if(c->model == KO_MODEL_QUADROTOR) return prop_quad_f(c, x0, u, obs, n_obs, x1);
-    return prop_di_f(c, x0, u, obs, n_obs, x1);
+    switch(c->model)
+        {
+            case KO_MODEL_QUADROTOR: return prop_quad_f(c, x0, u, obs, n_obs, x1);
+            case KO_MODEL_DUBINS_AIRPLANE: return prop_dubins_f(c, x0, u, obs, n_obs, x1);
+            case KO_MODEL_UNICYCLE: return prop_uni_f(c, x0, u, obs, n_obs, x1);
+            default: return prop_di_f(c, x0, u, obs, n_obs, x1);
+        }
+}
+
+static int propagate_one_d(const ko_config* c, const float* x0, const float* u, const float* obs, uint32_t n_obs, double* x1, double* m)
+{
+    switch(c->model)
+        {
+            case KO_MODEL_QUADROTOR: return prop_quad_d(c, x0, u, obs, n_obs, x1, m);
+            case KO_MODEL_DUBINS_AIRPLANE: return prop_dubins_d(c, x0, u, obs, n_obs, x1, m);
+            case KO_MODEL_UNICYCLE: return prop_uni_d(c, x0, u, obs, n_obs, x1, m);
+            default: return prop_di_d(c, x0, u, obs, n_obs, x1, m);
+        }
 }
 
 void ko_propagate_f32(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs, uint32_t n,
@@ -617,16 +862,14 @@ void ko_propagate_f64(const ko_config* c, const float* x0, const float* u, const
             const float* a = x0 + (size_t)i * D;
             const float* w = u + (size_t)i * 8;
             double* y = x1 + (size_t)i * D;
-            if(c->model == KO_MODEL_QUADROTOR) valid[i] = (uint8_t)prop_quad_d(c, a, w, obstacles, n_obs, y, NULL);
-            else valid[i] = (uint8_t)prop_di_d(c, a, w, obstacles, n_obs, y, NULL);
+            valid[i] = (uint8_t)propagate_one_d(c, a, w, obstacles, n_obs, y, NULL);
         }
 }
 
 double ko_verdict_margin_f64(const ko_config* c, const float* x0, const float* u, const float* obstacles, uint32_t n_obs)
 {
     double y[KO_MAX_SAMPLE_DIM], m = 1e30;
-    if(c->model == KO_MODEL_QUADROTOR) prop_quad_d(c, x0, u, obstacles, n_obs, y, &m);
-    else prop_di_d(c, x0, u, obstacles, n_obs, y, &m);
+    propagate_one_d(c, x0, u, obstacles, n_obs, y, &m);
     return m;
 }
 
@@ -639,10 +882,12 @@ void ko_score_update(const ko_config* c, const int32_t* counter, const int32_t* 
                      float* score, float* total_out)
 {
     uint32_t L = c->coarse_len, F = c->fine_len;
-    uint32_t R1 = L * L * L;
-    float F2 = (float)(F * F * F);
+    const int planar = ko_ws_dims(c->model) == 2;
+    uint32_t R1 = planar ? L * L : L * L * L;
+    float F2 = (float)(planar ? F * F : F * F * F);
     float size1 = (c->ws_max - c->ws_min) / (float)L;
-    float vol = (size1 * size1) * size1;
+    float area = size1 * size1;
+    float vol = planar ? area : area * size1; /* W_R1_VOL in the workspace dimension */
     float lanes[KO_SCORE_LANES];
     for(int l = 0; l < KO_SCORE_LANES; ++l) lanes[l] = 0.0f;
     for(uint32_t r = 0; r < R1; ++r)
@@ -699,8 +944,10 @@ int ko_plan(const ko_config* c, const float* init, const float* goal, const floa
     const uint32_t T = c->tree_capacity;
     const uint32_t S = c->samples_per_node;
     const uint32_t L = c->coarse_len;
-    const uint32_t R1 = L * L * L;
-    if(T < 2 || S < 1 || L < 1 || c->fine_len < 1 || c->fine_len * c->fine_len * c->fine_len > 64) return -1;
+    const int W = ko_ws_dims(c->model);
+    const uint32_t R1 = W == 2 ? L * L : L * L * L;
+    const uint32_t FC = W == 2 ? c->fine_len * c->fine_len : c->fine_len * c->fine_len * c->fine_len;
+    if(T < 2 || S < 1 || L < 1 || c->fine_len < 1 || FC > 64) return -1;
 
     int32_t* node_r1 = (int32_t*)calloc(T, sizeof(int32_t));
     uint32_t* rep_old = (uint32_t*)malloc(sizeof(uint32_t) * T);
@@ -801,7 +1048,7 @@ int ko_plan(const ko_config* c, const float* init, const float* goal, const floa
                     const float* y = us + (size_t)s * D;
                     for(int j = 0; j < D; ++j) samples[(size_t)idx * D + j] = y[j];
                     parents[idx] = up[s];
-                    float dist = ko_distance(y, goal);
+                    float dist = ko_distance_w(y, goal, W);
                     costs[idx] = dist;
                     node_r1[idx] = ur1[s];
                     uint32_t rep = validc[ur1[s]] < KO_SPARSE_VALID_LIMIT ? KO_NEW_NODE_REPEAT_SPARSE : KO_NEW_NODE_REPEAT_DENSE;
@@ -878,17 +1125,31 @@ int ko_plan_batch(uint32_t nq, const ko_config* cfgs, const float* inits, const 
             float* samples = (float*)malloc(sizeof(float) * (size_t)c->tree_capacity * D);
             int32_t* parents = (int32_t*)malloc(sizeof(int32_t) * c->tree_capacity);
             float* costs = (float*)malloc(sizeof(float) * c->tree_capacity);
-            if(!samples || !parents || !costs)
+            /* a planar query takes its boxes as rows of 4 (x, y extents) */
+            const float* rows = obstacles + 6 * (size_t)obs_offset[q];
+            float* rows2 = NULL;
+            if(ko_ws_dims(c->model) == 2 && obs_count[q] > 0)
+                {
+                    rows2 = (float*)malloc(sizeof(float) * 4 * (size_t)obs_count[q]);
+                    if(rows2)
+                        for(uint32_t o = 0; o < obs_count[q]; ++o)
+                            {
+                                rows2[4 * o + 0] = rows[6 * o + 0], rows2[4 * o + 1] = rows[6 * o + 1];
+                                rows2[4 * o + 2] = rows[6 * o + 3], rows2[4 * o + 3] = rows[6 * o + 4];
+                            }
+                    rows = rows2;
+                }
+            if(!samples || !parents || !costs || !rows)
                 {
                     err |= 1;
                 }
             else
                 {
-                    int rc = ko_plan(c, inits + (size_t)q * KO_MAX_SAMPLE_DIM, goals + (size_t)q * KO_MAX_SAMPLE_DIM,
-                                     obstacles + 6 * (size_t)obs_offset[q], obs_count[q], &res[q], samples, parents, costs, NULL, NULL);
+                    int rc = ko_plan(c, inits + (size_t)q * KO_MAX_SAMPLE_DIM, goals + (size_t)q * KO_MAX_SAMPLE_DIM, rows, obs_count[q],
+                                     &res[q], samples, parents, costs, NULL, NULL);
                     if(rc) err |= 1;
                 }
-            free(samples), free(parents), free(costs);
+            free(samples), free(parents), free(costs), free(rows2);
         }
     return err ? -1 : 0;
 }

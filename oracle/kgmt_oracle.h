@@ -9,7 +9,9 @@
  *   planner loop          src/planners/KGMT.cu:41-105, 167-211, 218-259, 305-403
  *   repeat expansion      src/planners/Planner.cu:52-79
  *   region ids / scores   src/graphs/Graph.cu:53-97, 99-153, 155-205, 311-358
- *   dynamics              src/statePropagator/statePropagator.cu:76-142, 246-370
+ *   dynamics              src/statePropagator/statePropagator.cu:13-74 (unicycle),
+ *                         76-142 (double integrator), 147-244 (Dubins airplane),
+ *                         246-370 (quadrotor)
  *   collision             src/collisionCheck/collisionCheck.cu:3-10, 49-61
  *   goal distance         include/helper/helper.cuh:138-152
  *
@@ -33,7 +35,9 @@
 extern "C" {
 #endif
 
+#define KO_MODEL_UNICYCLE 0          /* reference MODEL 0 (config.h), planar */
 #define KO_MODEL_DOUBLE_INTEGRATOR 1 /* reference MODEL 1 (config.h) */
+#define KO_MODEL_DUBINS_AIRPLANE 2   /* reference MODEL 2 (config.h) */
 #define KO_MODEL_QUADROTOR 3         /* reference MODEL 3 (config.h) */
 
 #define KO_DI_RULE_RK4 0       /* classic RK4 position update            */
@@ -72,6 +76,9 @@ typedef struct ko_config {
     float u_max[4];
     float nu, mu, ix, iy, iz, gravity, mass_inv;
     uint64_t seed;
+    float pitch_min, pitch_max; /* Dubins airplane */
+    float wheelbase;            /* unicycle */
+    uint32_t reserved;
 } ko_config;
 
 typedef struct ko_result {
@@ -109,10 +116,16 @@ int ko_state_dim(int32_t model);
 void ko_sample_uniforms(uint64_t seed, uint32_t slot, uint32_t itr, float u[8]);
 float ko_react_uniform(uint64_t seed, uint32_t node, uint32_t itr);
 
+/* workspace dimension W: 2 for the planar unicycle, else 3.  Obstacle boxes
+ * passed to the functions below are rows of 2W floats (min corner, max
+ * corner), as the reference lays them out (collisionCheck.cu:53-57), except
+ * in ko_plan_batch, whose rows are always 6 floats. */
+int ko_ws_dims(int32_t model);
 int ko_region(const ko_config* c, const float* x);
 int ko_subregion(const ko_config* c, const float* x, int r1);
-float ko_distance(const float* a, const float* b);
-int ko_segment_valid(const float* p0, const float* p1, const float* obstacles, uint32_t n_obs);
+float ko_distance(const float* a, const float* b);             /* 3-D */
+float ko_distance_w(const float* a, const float* b, int w);    /* first w components */
+int ko_segment_valid(const float* p0, const float* p1, const float* obstacles, uint32_t n_obs); /* 3-D */
 
 /* FP32 mirror propagation of n samples with explicit uniforms u[n*8].
  * x0: n*sample_dim, x1: n*sample_dim, valid: n bytes. */
@@ -137,8 +150,8 @@ int ko_plan(const ko_config* c, const float* init, const float* goal, const floa
             float* samples, int32_t* parents, float* costs, float* path, ko_iter_trace* trace);
 
 /* n independent queries; OpenMP over queries with `threads` threads (0 = all).
- * Only results (no trees) are returned.  obstacles concatenated, obs_offset
- * in obstacles (not floats). */
+ * Only results (no trees) are returned.  obstacles concatenated as rows of 6
+ * floats (a planar query uses the x and y extents), obs_offset in boxes. */
 int ko_plan_batch(uint32_t nq, const ko_config* cfgs, const float* inits, const float* goals, const float* obstacles,
                   const uint32_t* obs_offset, const uint32_t* obs_count, ko_result* res, int threads);
 int ko_max_threads(void);

@@ -26,6 +26,7 @@ class KoConfig(C.Structure):
         ("coarse_len", C.c_uint32), ("fine_len", C.c_uint32), ("v_min", C.c_float), ("v_max", C.c_float),
         ("u_min", C.c_float * 4), ("u_max", C.c_float * 4), ("nu", C.c_float), ("mu", C.c_float), ("ix", C.c_float),
         ("iy", C.c_float), ("iz", C.c_float), ("gravity", C.c_float), ("mass_inv", C.c_float), ("seed", C.c_uint64),
+        ("pitch_min", C.c_float), ("pitch_max", C.c_float), ("wheelbase", C.c_float), ("reserved", C.c_uint32),
     ]
 
 
@@ -137,7 +138,7 @@ def subregion(cfg, x, r1) -> int:
 
 
 def segment_valid(p0, p1, obstacles) -> int:
-    obs = _f32(obstacles).reshape(-1, 6)
+    obs = _f32(obstacles).reshape(-1, 6)  # 3-D
     return int(load().ko_segment_valid(_ptr(_f32(p0), C.c_float), _ptr(_f32(p1), C.c_float), _ptr(obs, C.c_float),
                                        obs.shape[0]))
 
@@ -146,12 +147,29 @@ def distance(a, b) -> float:
     return float(load().ko_distance(_ptr(_f32(a), C.c_float), _ptr(_f32(b), C.c_float)))
 
 
+def ws_dims(model: int) -> int:
+    return 2 if model == 0 else 3
+
+
+def boxes(cfg, obstacles) -> np.ndarray:
+    """Boxes in the model's layout, rows of 2W floats (min corner, max
+    corner).  A [m, 6] array given for a planar model keeps its x and y
+    extents; a flat array is taken as rows of 2W already."""
+    w = ws_dims(cfg.model)
+    a = _f32(obstacles)
+    if a.size == 0:
+        return np.zeros((0, 2 * w), np.float32)
+    if w == 2 and a.ndim == 2 and a.shape[1] == 6:
+        a = a[:, [0, 1, 3, 4]]
+    return np.ascontiguousarray(a.reshape(-1, 2 * w))
+
+
 def propagate_f32(cfg, x0, u, obstacles):
-    """x0 [n, D], u [n, 8], obstacles [m, 6] -> (x1 [n, D], valid [n], r1, r2)."""
+    """x0 [n, D], u [n, 8], obstacles [m, 6] or [m, 2W] -> (x1 [n, D], valid [n], r1, r2)."""
     k = to_ko(cfg)
     x0 = _f32(x0)
     u = _f32(u)
-    obs = _f32(obstacles).reshape(-1, 6)
+    obs = boxes(cfg, obstacles)
     n = x0.shape[0]
     x1 = np.zeros_like(x0)
     valid = np.zeros(n, np.uint8)
@@ -166,7 +184,7 @@ def propagate_f64(cfg, x0, u, obstacles):
     k = to_ko(cfg)
     x0 = _f32(x0)
     u = _f32(u)
-    obs = _f32(obstacles).reshape(-1, 6)
+    obs = boxes(cfg, obstacles)
     n = x0.shape[0]
     x1 = np.zeros(x0.shape, np.float64)
     valid = np.zeros(n, np.uint8)
@@ -177,7 +195,7 @@ def propagate_f64(cfg, x0, u, obstacles):
 
 def verdict_margin_f64(cfg, x0, u, obstacles) -> float:
     k = to_ko(cfg)
-    obs = _f32(obstacles).reshape(-1, 6)
+    obs = boxes(cfg, obstacles)
     return float(load().ko_verdict_margin_f64(C.byref(k), _ptr(_f32(x0), C.c_float), _ptr(_f32(u), C.c_float),
                                            _ptr(obs, C.c_float), obs.shape[0]))
 
@@ -213,7 +231,7 @@ def plan(query, trace: bool = False):
     res = KoResult()
     init = _f32(query.init)
     goal = _f32(query.goal)
-    obs = _f32(query.obstacles).reshape(-1, 6)
+    obs = boxes(cfg, query.obstacles)
     rc = load().ko_plan(C.byref(k), _ptr(init, C.c_float), _ptr(goal, C.c_float), _ptr(obs, C.c_float), obs.shape[0],
                         C.byref(res), _ptr(samples, C.c_float), _ptr(parents, C.c_int32), _ptr(costs, C.c_float),
                         _ptr(path, C.c_float), tr)

@@ -12,15 +12,22 @@
 #define NUM_PARTIAL_SUMS 1024
 #define EPSILON 1e-2f
 #define VERBOSE 0
-#define UNI_MIN_STEERING -M_PI / 2
-#define UNI_MAX_STEERING M_PI / 2
+/* The reference writes these bounds as double expressions (-M_PI / 2, ...),
+ * which makes its control draws MIN + u * (MAX - MIN) double arithmetic
+ * rounded to float once, while a runtime float config rounds each step.
+ * Near steering +-pi/2 one ulp of steering moves tan(steering) by ~1e-4
+ * relative, so the golden configs give the same values as float literals
+ * (pi/2, pi/4, pi/3 rounded to float): the fixtures then compare the
+ * dynamics, not the rounding of a bound. */
+#define UNI_MIN_STEERING (-0x1.921fb6p+0f)
+#define UNI_MAX_STEERING (0x1.921fb6p+0f)
 #define UNI_MIN_DT 0.1f
 #define UNI_MAX_DT 2.0f
 #define UNI_LENGTH 1.0f
-#define DUBINS_AIRPLANE_MIN_PR (-M_PI / 4)
-#define DUBINS_AIRPLANE_MAX_PR (M_PI / 4)
-#define DUBINS_AIRPLANE_MIN_YR (-M_PI / 4)
-#define DUBINS_AIRPLANE_MAX_YR (M_PI / 4)
-#define DUBINS_AIRPLANE_MIN_PITCH -M_PI / 3
-#define DUBINS_AIRPLANE_MAX_PITCH M_PI / 3
+#define DUBINS_AIRPLANE_MIN_PR (-0x1.921fb6p-1f)
+#define DUBINS_AIRPLANE_MAX_PR (0x1.921fb6p-1f)
+#define DUBINS_AIRPLANE_MIN_YR (-0x1.921fb6p-1f)
+#define DUBINS_AIRPLANE_MAX_YR (0x1.921fb6p-1f)
+#define DUBINS_AIRPLANE_MIN_PITCH (-0x1.0c1524p+0f)
+#define DUBINS_AIRPLANE_MAX_PITCH (0x1.0c1524p+0f)
 #define KM 0.03f

@@ -14,6 +14,8 @@ Fixtures:
   ref_di.npz     reference DI propagation (statePropagator.cu:76-142), its
                  position formula (statePropagator.cu:97-99) as written
   ref_quad.npz   reference quadrotor propagation (statePropagator.cu:246-370)
+  ref_dubins.npz reference Dubins-airplane propagation (statePropagator.cu:147-244)
+  ref_unicycle.npz reference unicycle propagation (statePropagator.cu:13-74)
   ref_collision.npz  isMotionValid verdicts (collisionCheck.cu:3-10, 49-61)
   ref_region.npz getRegion ids (Graph.cu:99-153), 8^3 and 16^3 grids
   philox_kat.json published Philox4x32-10 known-answer vectors (Random123)
@@ -47,10 +49,10 @@ def fp(a):
 def load_ref(ref: str):
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle" / "ref"), f"REF={ref}"], check=True)
     libs = {}
-    for name in ("di", "quad", "graph_di", "graph_quad"):
+    for name in ("di", "quad", "dubins", "uni", "graph_di", "graph_quad"):
         lib = C.CDLL(str(REF_LIB / f"libref_{name}.so"))
         libs[name] = lib
-    for k in ("di", "quad"):
+    for k in ("di", "quad", "dubins", "uni"):
         libs[k].ref_propagate.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_int, C.POINTER(C.c_float)]
         libs[k].ref_motion_valid.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_int]
     for k in ("graph_di", "graph_quad"):
@@ -118,6 +120,48 @@ def quad_fixture(lib):
     x0[1, 3:12] = 0.0
     x1, valid = make_dynamics(lib, cfg, x0, u, q.obstacles)
     np.savez_compressed(OUT / "ref_quad.npz", x0=x0, u=u, obstacles=q.obstacles, x1=x1, valid=valid)
+    return valid.mean()
+
+
+def dubins_fixture(lib):
+    q = W.dubins_query(seed=3, n_obstacles=40)
+    rng = np.random.Generator(np.random.Philox(key=20240605))
+    n = 1500
+    x0 = np.zeros((n, 10), np.float32)
+    x0[:, :3] = rng.uniform(0.1, 0.9, (n, 3))
+    x0[:, 3] = rng.uniform(-np.pi, np.pi, n)
+    x0[:, 4] = rng.uniform(-1.0, 1.0, n)
+    x0[:, 5] = rng.uniform(0.0, 0.3, n)
+    u = uniforms(779, n)
+    u[:, 3] = np.minimum(u[:, 3], np.float32(1.0 - 2.0 ** -24))
+    u[0, 3] = 2.0 ** -24  # k = 1
+    u[1, 3] = 1.0 - 2.0 ** -24  # k = 10
+    x0[2, 5] = 0.0  # at rest
+    x0[3, 4] = 1.04  # pitch near its bound
+    x1, valid = make_dynamics(lib, q.config, x0, u, q.obstacles)
+    np.savez_compressed(OUT / "ref_dubins.npz", x0=x0, u=u, obstacles=q.obstacles, x1=x1, valid=valid)
+    return valid.mean()
+
+
+def unicycle_fixture(lib):
+    # the reference's unicycle compiles with W_DIM 3 here: its step boxes lie
+    # in z = 0, so boxes spanning z in [-1, 1] give the planar verdict
+    q = W.unicycle_query(seed=3, n_obstacles=40)
+    obs = q.obstacles.copy()
+    obs[:, 2], obs[:, 5] = -1.0, 1.0
+    rng = np.random.Generator(np.random.Philox(key=20240606))
+    n = 1500
+    x0 = np.zeros((n, 7), np.float32)
+    x0[:, :2] = rng.uniform(0.1, 0.9, (n, 2))
+    x0[:, 2] = rng.uniform(-np.pi, np.pi, n)
+    x0[:, 3] = rng.uniform(0.0, 0.3, n)
+    u = uniforms(780, n)
+    u[:, 3] = np.minimum(u[:, 3], np.float32(1.0 - 2.0 ** -24))
+    u[0, 3] = 2.0 ** -24
+    u[1, 3] = 1.0 - 2.0 ** -24
+    x0[2, 3] = 0.0
+    x1, valid = make_dynamics(lib, q.config, x0, u, obs)
+    np.savez_compressed(OUT / "ref_unicycle.npz", x0=x0, u=u, obstacles=obs, x1=x1, valid=valid)
     return valid.mean()
 
 
@@ -189,8 +233,11 @@ def main():
     args = ap.parse_args()
     libs = load_ref(args.ref)
     assert libs["di"].ref_model() == 1 and libs["quad"].ref_model() == 3
+    assert libs["dubins"].ref_model() == 2 and libs["uni"].ref_model() == 0
     print("di valid fraction", di_fixture(libs["di"]))
     print("quad valid fraction", quad_fixture(libs["quad"]))
+    print("dubins valid fraction", dubins_fixture(libs["dubins"]))
+    print("unicycle valid fraction", unicycle_fixture(libs["uni"]))
     print("collision valid fraction", collision_fixture(libs["di"]))
     region_fixture(libs)
     philox_kat()

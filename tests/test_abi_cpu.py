@@ -12,7 +12,7 @@ import pytest
 
 from kgmt_gb300 import _abi
 from kgmt_gb300.build import build
-from kgmt_gb300.config import PlannerConfig, double_integrator_single, quadrotor_large
+from kgmt_gb300.config import PlannerConfig, double_integrator_single, dubins_airplane, quadrotor_large, unicycle
 
 ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "kgmt.h"
@@ -83,8 +83,20 @@ def test_config_defaults_and_validation(lib):
     assert (c.coarse_len, c.fine_len, c.tree_capacity, c.min_steps, c.max_steps) == (16, 4, 2_000_000, 3, 15)
     assert c.gravity == pytest.approx(q.gravity)
     assert lib.kgmt_config_default(7, C.byref(c)) == 1
-    bad = [dict(model=2), dict(tree_capacity=1), dict(samples_per_node=0), dict(min_steps=0), dict(min_steps=7, max_steps=6),
-           dict(fine_len=5), dict(ws_max=0.0), dict(step_size=0.0), dict(coarse_len=0), dict(di_rule=3)]
+    # the Dubins airplane and unicycle defaults are the Python presets
+    for model, preset in ((2, dubins_airplane()), (0, unicycle())):
+        assert lib.kgmt_config_default(model, C.byref(c)) == 0
+        ours = _abi.to_c(preset)
+        for name, _ in _abi.KgmtConfig._fields_:
+            if name in ("u_min", "u_max"):
+                assert list(getattr(c, name))[:3] == pytest.approx(list(getattr(ours, name))[:3]), (model, name)
+            elif name not in ("seed", "nu", "mu", "ix", "iy", "iz", "gravity", "mass_inv", "di_rule"):
+                assert getattr(c, name) == pytest.approx(getattr(ours, name)), (model, name)
+        assert lib.kgmt_config_validate(C.byref(c)) == 0
+        assert lib.kgmt_sample_dim(model) == preset.sample_dim
+    bad = [dict(model=4), dict(model=-1), dict(tree_capacity=1), dict(samples_per_node=0), dict(min_steps=0),
+           dict(min_steps=7, max_steps=6), dict(fine_len=5), dict(ws_max=0.0), dict(step_size=0.0), dict(coarse_len=0),
+           dict(di_rule=3), dict(model=0, fine_len=9), dict(model=0, wheelbase=0.0), dict(model=2, pitch_min=1.0, pitch_max=0.0)]
     for kw in bad:
         k = _abi.to_c(PlannerConfig().replace(**kw))
         assert lib.kgmt_config_validate(C.byref(k)) == 1, kw
@@ -99,7 +111,12 @@ def test_query_bytes(lib):
     # tree + unexplored rows dominate: capacity x (2 x 40 B + 6 x 4 B + 1 B)
     assert 100_000 * 105 <= b0 <= 100_000 * 125
     assert b10 > b0
-    assert lib.kgmt_sample_dim(1) == 10 and lib.kgmt_sample_dim(3) == 17 and lib.kgmt_sample_dim(0) == -1
+    assert lib.kgmt_sample_dim(1) == 10 and lib.kgmt_sample_dim(3) == 17
+    assert lib.kgmt_sample_dim(0) == 7 and lib.kgmt_sample_dim(2) == 10 and lib.kgmt_sample_dim(4) == -1
+    # the unicycle's 7-float rows (T = 100k, as the double integrator's 10)
+    u = _abi.to_c(unicycle())
+    bu = lib.kgmt_query_bytes(C.byref(u), 0)
+    assert 100_000 * 80 <= bu < b0 - 100_000 * 2 * 12 + 1
 
 
 def test_no_device_fails_loudly(lib):

@@ -10,7 +10,8 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from kgmt_gb300 import workloads as W
-from kgmt_gb300.config import DI_RULE_REFERENCE, double_integrator_single, quadrotor_large
+from kgmt_gb300.config import (DI_RULE_REFERENCE, MODEL_DUBINS_AIRPLANE, MODEL_UNICYCLE, double_integrator_single,
+                               dubins_airplane, quadrotor_large, unicycle)
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -31,7 +32,14 @@ def state_scales(cfg):
     D = cfg.sample_dim
     s = np.ones(D)
     s[:3] = cfg.ws_max - cfg.ws_min
-    if D == 10:
+    if cfg.model == MODEL_UNICYCLE:  # x y theta v | a steering dt
+        s[2] = np.pi
+        s[3] = 0.3
+    elif cfg.model == MODEL_DUBINS_AIRPLANE:  # x y z yaw pitch v | yr pr a | k h
+        s[3:5] = np.pi
+        s[5] = cfg.v_max
+        s[9] = cfg.step_size
+    elif D == 10:
         s[3:6] = cfg.v_max
         s[9] = cfg.step_size
     else:
@@ -46,7 +54,7 @@ def gpu_propagate(cfg, x0, u, obs):
     n, D = x0.shape
     d_x0 = torch.from_numpy(np.ascontiguousarray(x0, np.float32)).to(DEV)
     d_u = torch.from_numpy(np.ascontiguousarray(u, np.float32)).to(DEV)
-    d_obs = torch.from_numpy(np.ascontiguousarray(obs, np.float32).reshape(-1, 6)).to(DEV)
+    d_obs = torch.from_numpy(O.boxes(cfg, obs)).to(DEV)  # rows of 2W floats, the model's layout
     d_x1 = torch.zeros((n, D), dtype=torch.float32, device=DEV)
     d_valid = torch.zeros(n, dtype=torch.uint8, device=DEV)
     d_r1 = torch.zeros(n, dtype=torch.int32, device=DEV)
@@ -61,7 +69,14 @@ def random_inputs(cfg, n, seed):
     D = cfg.sample_dim
     x0 = np.zeros((n, D), np.float32)
     x0[:, :3] = rng.uniform(0.05, 0.95, (n, 3))
-    if D == 10:
+    if cfg.model == MODEL_UNICYCLE:
+        x0[:, 2] = rng.uniform(-np.pi, np.pi, n)
+        x0[:, 3] = rng.uniform(0.0, 0.3, n)
+    elif cfg.model == MODEL_DUBINS_AIRPLANE:
+        x0[:, 3] = rng.uniform(-np.pi, np.pi, n)
+        x0[:, 4] = rng.uniform(-1.0, 1.0, n)
+        x0[:, 5] = rng.uniform(0.0, 0.3, n)
+    elif D == 10:
         x0[:, 3:6] = rng.uniform(-0.3, 0.3, (n, 3))
     else:
         x0[:, 3:6] = rng.uniform(-0.6, 0.6, (n, 3))
@@ -97,9 +112,25 @@ def test_propagate_quad_bit_exact_vs_oracle():
     assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
 
 
-@pytest.mark.parametrize("model", ["di", "quad"])
+@pytest.mark.parametrize("make", [W.dubins_query, W.unicycle_query], ids=["dubins", "unicycle"])
+def test_propagate_new_models_bit_exact_vs_oracle(make):
+    q = make(seed=2, n_obstacles=40)
+    cfg = q.config
+    x0, u = random_inputs(cfg, 4096, 14)
+    gx, gv, g1, g2 = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, o1, o2 = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert 0.05 < ov.mean() < 0.95
+    assert np.array_equal(gv, ov)
+    assert np.array_equal(gx.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
+
+
+QUERIES = {"di": W.double_integrator_query, "quad": W.quadrotor_query, "dubins": W.dubins_query, "unicycle": W.unicycle_query}
+
+
+@pytest.mark.parametrize("model", ["di", "quad", "dubins", "unicycle"])
 def test_propagate_within_tolerance_of_fp64(model):
-    q = W.double_integrator_query(seed=3) if model == "di" else W.quadrotor_query(seed=3)
+    q = QUERIES[model](seed=3)
     cfg = q.config
     x0, u = random_inputs(cfg, 4096, 13)
     gx, gv, _, _ = gpu_propagate(cfg, x0, u, q.obstacles)
@@ -131,6 +162,16 @@ def test_propagate_matches_reference_golden(golden_dir):
     assert same.mean() > 0.99
     tol = REL_TOL * np.maximum(np.abs(gq["x1"]), state_scales(cq))
     assert np.all(np.abs(qx - gq["x1"])[same] <= tol[same])
+    # Dubins airplane and unicycle: the reference's own code fed the same
+    # uniforms (its unicycle boxes span z in [-1, 1]; ours are planar)
+    for name, cfg in (("ref_dubins.npz", dubins_airplane(seed=3)), ("ref_unicycle.npz", unicycle(seed=3))):
+        g = np.load(golden_dir / name)
+        x, v, _, _ = gpu_propagate(cfg, g["x0"], g["u"], g["obstacles"])
+        same = v == g["valid"]
+        for i in np.flatnonzero(~same):
+            assert O.verdict_margin_f64(cfg, g["x0"][i], g["u"][i], g["obstacles"]) < 1e-6, (name, i)
+        tol = REL_TOL * np.maximum(np.abs(g["x1"]), state_scales(cfg))
+        assert np.all(np.abs(x - g["x1"])[same] <= tol[same]), name
 
 
 # ---------------------------------------------------------------------------
@@ -138,7 +179,7 @@ def test_propagate_matches_reference_golden(golden_dir):
 # ---------------------------------------------------------------------------
 def plan_gpu(q):
     from kgmt_gb300.planner import KGMT
-    d_obs = torch.from_numpy(np.ascontiguousarray(q.obstacles, np.float32).reshape(-1, 6)).to(DEV)
+    d_obs = torch.from_numpy(np.ascontiguousarray(W.boxes_for_plan(q), np.float32)).to(DEV)
     p = KGMT(q.config)
     res = p.plan(q.init, q.goal, d_obs, q.obstacles.shape[0])
     samples, parents, costs = p.copy_tree()
@@ -172,6 +213,39 @@ def test_plan_double_integrator_reference_rule_bit_exact():
 def test_plan_quadrotor_small_bit_exact():
     q = W.quadrotor_query(seed=1, tree_capacity=30_000, max_iterations=25)
     assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_plan_dubins_bit_exact(seed):
+    q = W.dubins_query(seed=seed, tree_capacity=40_000)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_plan_unicycle_bit_exact(seed):
+    """Planar model: the single-query plan takes the reference's [n][4] box
+    rows; regions are 8^2 with 4^2 fine cells."""
+    q = W.unicycle_query(seed=seed, tree_capacity=40_000)
+    assert_same_plan(*plan_gpu(q), O.plan(q))
+
+
+def test_batch_all_models_matches_oracle():
+    """The four models in one batch (the mixed propagate variant); each query
+    as its oracle plan, and as the same query planned alone."""
+    qs = W.all_models_batch(16, seed=4, tree_capacity=20_000)
+    for q in qs:
+        q.config = q.config.replace(max_iterations=40)
+    b, res = _batch(qs)
+    refs = O.plan_batch(qs)
+    for i, (r, ref) in enumerate(zip(res, refs)):
+        for k in ("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn"):
+            assert r[k] == ref[k], (i, k, r[k], ref[k])
+    for i in (0, 2):
+        alone = plan_gpu(qs[i])
+        s, p, c = b.copy_tree(i)
+        n = res[i]["tree_size"]
+        assert np.array_equal(p[:n], alone[2])
+        assert np.array_equal(s[:n].view(np.uint32), alone[1].view(np.uint32))
 
 
 def test_plan_edge_cases():

@@ -6,7 +6,8 @@ import json
 import numpy as np
 import pytest
 
-from kgmt_gb300.config import DI_RULE_REFERENCE, double_integrator_single, quadrotor_large
+from kgmt_gb300.config import (DI_RULE_REFERENCE, MODEL_DUBINS_AIRPLANE, MODEL_UNICYCLE, double_integrator_single,
+                               dubins_airplane, quadrotor_large, unicycle)
 from oracle import oracle as O
 
 # state tolerance: |delta| <= 1e-5 * max(|ref|, scale) per component
@@ -17,7 +18,14 @@ def state_scales(cfg):
     D = cfg.sample_dim
     s = np.ones(D)
     s[:3] = cfg.ws_max - cfg.ws_min
-    if D == 10:
+    if cfg.model == MODEL_UNICYCLE:  # x y theta v | a steering dt
+        s[2] = np.pi
+        s[3] = 0.3
+    elif cfg.model == MODEL_DUBINS_AIRPLANE:  # x y z yaw pitch v | yr pr a | k h
+        s[3:5] = np.pi
+        s[5] = cfg.v_max
+        s[9] = cfg.step_size
+    elif D == 10:
         s[3:6] = cfg.v_max
         s[6:9] = 1.0
         s[9] = cfg.step_size
@@ -72,6 +80,46 @@ def test_quad_matches_reference_within_tolerance(golden_dir):
         tol = REL_TOL * np.maximum(np.abs(g["x1"]), state_scales(cfg))
         bad = np.abs(x1[same] - g["x1"][same]) > tol[same]
         assert not bad.any(), (fn.__name__, np.argwhere(bad)[:5])
+
+
+@pytest.mark.parametrize("fixture,cfg", [("ref_dubins.npz", dubins_airplane(seed=3)), ("ref_unicycle.npz", unicycle(seed=3))])
+def test_new_models_match_reference_within_tolerance(golden_dir, fixture, cfg):
+    """Dubins airplane (statePropagator.cu:147-244) and unicycle (13-74): the
+    FP32 mirror (portable sine/cosine) and the FP64 restatement against the
+    reference's own code fed the same uniforms.  Verdicts agree except where
+    the FP64 trajectory passes within 1e-6 of a bound or a box face."""
+    g = np.load(golden_dir / fixture)
+    for fn in (O.propagate_f32, O.propagate_f64):
+        out = fn(cfg, g["x0"], g["u"], g["obstacles"])
+        x1, valid = out[0], out[1]
+        same = valid == g["valid"]
+        for i in np.flatnonzero(~same):
+            assert O.verdict_margin_f64(cfg, g["x0"][i], g["u"][i], g["obstacles"]) < 1e-6, (fn.__name__, i)
+        assert same.mean() > 0.99, fn.__name__
+        tol = REL_TOL * np.maximum(np.abs(g["x1"]), state_scales(cfg))
+        bad = np.abs(x1[same] - g["x1"][same]) > tol[same]
+        assert not bad.any(), (fn.__name__, np.argwhere(bad)[:5])
+    assert 0.2 < g["valid"].mean() < 0.9  # the fixture exercises both verdicts
+
+
+def test_planar_regions():
+    """W_DIM 2 (unicycle): r1 = ix * L + iy (Graph.cu:105-113 with two
+    workspace digits), fine cell jx * F + jy; the heading plays no part."""
+    cfg = unicycle()
+    L, F = cfg.coarse_len, cfg.fine_len
+    rng = np.random.default_rng(5)
+    for _ in range(500):
+        x = np.zeros(7, np.float32)
+        x[:2] = rng.uniform(-0.05, 1.05, 2)
+        x[2] = rng.uniform(-10, 10)
+        ix, iy = [min(max(int(np.float32(L) * x[d] / np.float32(1.0)), 0), L - 1) if x[d] >= 0 else 0 for d in range(2)]
+        r1 = O.region(cfg, x)
+        assert r1 == ix * L + iy
+        r2 = O.subregion(cfg, x, r1)
+        assert 0 <= r2 < F * F
+        y = x.copy()
+        y[2] = 0.0
+        assert O.region(cfg, y) == r1 and O.subregion(cfg, y, r1) == r2
 
 
 def test_collision_verdicts_bit_exact(golden_dir):
