@@ -551,6 +551,15 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
             const CellIds cid = cell_ids(p, x1);
             r1 = cid.r1;
             bit = 1ull << cid.r2;
+            // the region's marks and score are loaded before the row stores
+            // (which the compiler must otherwise keep ahead of them)
+            uint64_t marks = 0ull;
+            float score = 0.0f;
+            if(ok)
+                {
+                    marks = p.marks[r1];
+                    score = p.score[r1];
+                }
             float* dst = p.us + (size_t)s * D;
 #pragma unroll
             for(int j = 0; j < D; ++j) dst[j] = x1[j];
@@ -558,8 +567,8 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
             p.ur1[s] = r1;
             if(ok)
                 {
-                    const bool fresh = (p.marks[r1] & bit) == 0ull;
-                    acc = (u[NC + 1] < p.score[r1]) || fresh;
+                    const bool fresh = (marks & bit) == 0ull;
+                    acc = (u[NC + 1] < score) || fresh;
                 }
             p.uflag[s] = acc ? 1 : 0;
         }
@@ -883,6 +892,32 @@ __device__ void finalize_query(const QueryParams& p, QueryState& st, Sched* sche
     plan_samples(p, st);
 }
 
+// Copies one sample row (written by the propagate kernel, read-only here)
+// into the tree and returns its goal distance.  The row is read into
+// registers before the first store: the two buffers might alias as far as
+// the compiler can tell, so interleaved loads would each wait for the
+// previous store's turn.
+template <int D>
+__device__ __forceinline__ float append_row_d(const QueryParams& p, const float* src, float* dst)
+{
+    float r[D];
+#pragma unroll
+    for(int c = 0; c < D; ++c) r[c] = __ldg(src + c);
+#pragma unroll
+    for(int c = 0; c < D; ++c) dst[c] = r[c];
+    return goal_distance(p, r);
+}
+
+__device__ __forceinline__ float append_row(const QueryParams& p, const float* src, float* dst, int D)
+{
+    switch(D)
+        {
+            case 7: return append_row_d<7>(p, src, dst);
+            case 17: return append_row_d<17>(p, src, dst);
+            default: return append_row_d<10>(p, src, dst);
+        }
+}
+
 // KGMT.cu:387-388
 __device__ __forceinline__ float f_accept_of(const QueryParams& p, const QueryState& st)
 {
@@ -1004,13 +1039,13 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                             if(!(acc_bits & (1u << j))) continue;
                             const uint32_t s = s0 + j;
                             const uint32_t idx = ia++;
-                            const float* src = p.us + (size_t)s * D;
-                            float* dst = p.tree + (size_t)idx * D;
-                            for(int c = 0; c < D; ++c) dst[c] = src[c];
-                            p.parent[idx] = p.up[s];
-                            const float dist = goal_distance(p, src);
+                            // everything the sample needs is loaded before its
+                            // first store (one round trip, not one per field)
+                            const int32_t par = __ldg(p.up + s), r1 = __ldg(p.ur1 + s);
+                            const float dist = append_row(p, p.us + (size_t)s * D, p.tree + (size_t)idx * D, D);
+                            p.parent[idx] = par;
                             p.cost[idx] = dist;
-                            p.node_r1[idx] = p.ur1[s];
+                            p.node_r1[idx] = r1;
                             for(uint32_t r = 0; r < w[j]; ++r, ++iw)
                                 if(iw < p.capacity) p.rep_new[iw] = idx;
                             if(dist < p.goal_radius) atomicMin(&st.goal_cand, (int)idx);
