@@ -383,7 +383,9 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     KGMT_CUDA(cudaMemsetAsync(d_tile_a_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_c_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_old_, 0, sizeof(uint32_t) * slots, stream_), "memset");
-    KGMT_CUDA(cudaMallocHost(&h_running_, sizeof(uint32_t) * 2), "cudaMallocHost");
+    // the running count, written by the device into mapped pinned memory
+    KGMT_CUDA(cudaHostAlloc((void**)&h_running_, sizeof(uint32_t) * 2, cudaHostAllocMapped), "cudaHostAlloc(mapped)");
+    KGMT_CUDA(cudaHostGetDevicePointer((void**)&d_running_, h_running_, 0), "cudaHostGetDevicePointer");
     for(auto& e : ev_) KGMT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
     return set_prop_block(prop_block ? prop_block : 256);
 }
@@ -404,6 +406,7 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     Sched s;
     std::memset(&s, 0, sizeof(s));
     s.prop_tile = block;
+    s.host_running = d_running_;
     KGMT_CUDA(cudaMemcpyAsync(d_sched_, &s, sizeof(s), cudaMemcpyHostToDevice, stream_), "upload(sched)");
     KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");
     if(graph_)
@@ -593,19 +596,22 @@ kgmt_status Engine::launch_unit()
 
 kgmt_status Engine::run_until_done(uint32_t max_iters)
 {
+    // Units are launched one ahead of the poll: after unit u-1 completes, the
+    // running count the last schedule wrote (unit u-1's or a later one's) is
+    // read from the mapped host word; nothing but the event record sits in
+    // the stream between two graph replays.
     const uint32_t G = iters_per_graph_;
     const uint32_t max_units = (max_iters + G - 1) / G + 2;
+    volatile uint32_t* running = h_running_;
     for(uint32_t u = 0; u < max_units; ++u)
         {
             kgmt_status st = launch_unit();
             if(st != KGMT_OK) return st;
-            KGMT_CUDA(cudaMemcpyAsync(&h_running_[u & 1], &d_sched_->running, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_),
-                      "poll(running)");
             KGMT_CUDA(cudaEventRecord(ev_[u & 1], stream_), "cudaEventRecord");
             if(u > 0)
                 {
                     KGMT_CUDA(cudaEventSynchronize(ev_[(u - 1) & 1]), "cudaEventSynchronize");
-                    if(h_running_[(u - 1) & 1] == 0) break;
+                    if(*running == 0) break;
                 }
         }
     KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");

@@ -132,7 +132,8 @@ class Engine {
     uint32_t* d_tile_a_ = nullptr;
     uint32_t* d_tile_c_ = nullptr;
     uint32_t* d_tile_old_ = nullptr;
-    uint32_t* h_running_ = nullptr;  // pinned, 2 entries
+    uint32_t* h_running_ = nullptr;  // mapped pinned host word the device writes (Sched::host_running)
+    uint32_t* d_running_ = nullptr;  // its device address
     cudaEvent_t ev_[2] = {nullptr, nullptr};
     cudaGraphExec_t graph_ = nullptr;
     std::vector<QueryParams> h_params_;

@@ -292,6 +292,7 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
             sched->running = carry[2];
             sched->ticket_a = 0;
             if(carry[2]) sched->iterations += 1;
+            if(sched->host_running) *(volatile uint32_t*)sched->host_running = carry[2];
         }
     __syncthreads();
 }

@@ -160,6 +160,9 @@ struct Sched {
     uint32_t error;
     uint32_t iterations;  // engine iterations launched with work
     uint32_t prop_tile;   // samples per propagate tile (= propagate block size)
+    // mapped pinned host word that mirrors `running` (or null): the host polls
+    // it without a copy in the stream between graph replays
+    uint32_t* host_running;
 };
 
 }  // namespace kgmt
