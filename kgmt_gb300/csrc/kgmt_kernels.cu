@@ -249,6 +249,51 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
     __shared__ uint32_t carry[3];
     const int n = (int)sched->n_slots;
     const uint32_t prop_tile = sched->prop_tile;
+    if(n <= 32)
+        {
+            // up to 32 slots: one warp, shuffle scans, no block barriers but the last
+            if(threadIdx.x < 32)
+                {
+                    const int q = (int)threadIdx.x;
+                    uint32_t ta = 0, tc = 0, told = 0, run = 0;
+                    if(q < n && __ldcg(&S[q].status) == KGMT_QUERY_RUNNING)
+                        {
+                            const uint32_t ns = __ldcg(&S[q].n_samples);
+                            ta = (ns + prop_tile - 1) / prop_tile;
+                            told = (__ldcg(&S[q].tree_size) + kTileC - 1) / kTileC;
+                            tc = told + (ns + kTileC - 1) / kTileC;
+                            run = 1;
+                        }
+                    uint32_t ia = ta, ic = tc, ir = run;
+#pragma unroll
+                    for(int o = 1; o < 32; o <<= 1)
+                        {
+                            const uint32_t ya = __shfl_up_sync(0xffffffffu, ia, o);
+                            const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
+                            const uint32_t yr = __shfl_up_sync(0xffffffffu, ir, o);
+                            if(q >= o) ia += ya, ic += yc, ir += yr;
+                        }
+                    if(q < n)
+                        {
+                            tile_a_base[q] = ia - ta;
+                            tile_c_base[q] = ic - tc;
+                            tile_c_old[q] = told;
+                        }
+                    if(q == 31)
+                        {
+                            tile_a_base[n] = ia;
+                            tile_c_base[n] = ic;
+                            sched->tiles_a = ia;
+                            sched->tiles_c = ic;
+                            sched->running = ir;
+                            sched->ticket_a = 0;
+                            if(ir) sched->iterations += 1;
+                            if(sched->host_running) *(volatile uint32_t*)sched->host_running = ir;
+                        }
+                }
+            __syncthreads();
+            return;
+        }
     if(threadIdx.x == 0) carry[0] = carry[1] = carry[2] = 0;
     __syncthreads();
     for(int base = 0; base < n; base += blockDim.x)
@@ -945,7 +990,10 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
     // after every tile is done)
     const BaseCache cbase = cache_bases(tile_c_base, n_slots, s_cbase);
     const BaseCache cold = cache_bases(tile_c_old, n_slots - 1, s_cold);
-    uint32_t next = blockIdx.x;  // first tile static, then tickets
+    // First tile static, then tickets, taken only when the block is free: a
+    // ticket taken ahead would hold a tile that its successors' look-back
+    // waits for behind the block's current tile.
+    uint32_t next = blockIdx.x;
     for(;;)
         {
             if(threadIdx.x == 0)
@@ -1059,30 +1107,32 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     __threadfence();
                     const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
                     const uint32_t done = atomicAdd(&st.tiles_done, 1u);
+                    // the block is free now: its next ticket, in flight with the count
+                    next = gridDim.x + atomicAdd(&sched->ticket_c, 1u);
                     if(done == n_tiles - 1)
                         {
                             __threadfence();
-                            if(threadIdx.x == 0) st.f_accept = s_fa;
+                            st.f_accept = s_fa;
                             finalize_query(p, st, sched);
                             s_fin = 1;
                         }
-                    next = gridDim.x + atomicAdd(&sched->ticket_c, 1u);
                 }
             __syncthreads();
             if(s_fin)
                 {
-                    // every tile of this query is done: clear its look-back
-                    // words for the next iteration, then count it finalised
-                    const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
-                    for(uint32_t i = threadIdx.x; i < n_old; i += kAppendThreads) p.tiles_old[i] = 0ull;
-                    for(uint32_t i = threadIdx.x; i < n_tiles - n_old; i += kAppendThreads) p.tiles_slot[i] = 0ull;
-                    __syncthreads();
+                    // every tile of this query is done: count it finalised,
+                    // then clear its look-back words for the next iteration
+                    // (nothing in this kernel reads them again, and the next
+                    // append launch sees the stores: no fence on the path)
                     if(threadIdx.x == 0)
                         {
                             __threadfence();
                             const uint32_t f = atomicAdd(&sched->finalized, 1u);
                             if(f == sched->running - 1) s_glob = 1;
                         }
+                    const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
+                    for(uint32_t i = threadIdx.x; i < n_old; i += kAppendThreads) p.tiles_old[i] = 0ull;
+                    for(uint32_t i = threadIdx.x; i < n_tiles - n_old; i += kAppendThreads) p.tiles_slot[i] = 0ull;
                     __syncthreads();
                 }
             if(s_glob)
