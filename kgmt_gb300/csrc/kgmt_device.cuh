@@ -111,12 +111,13 @@ __device__ __forceinline__ float div_maybe_pow2(float x, float d, float inv_d, b
 // significant, Graph.cu:105-113); the fine cell is located relative to the
 // exact corner ws_min + idx * cell_size.
 // ---------------------------------------------------------------------------
+// clamp(trunc(t), 0, len - 1), with NaN and negative t giving 0: the
+// reference's `(int)t` then two clamps (Graph.cu:107-109) for every t in
+// range.  Branch-free: fmaxf returns 0 for a NaN t, and truncating the
+// clamped float equals clamping the truncated one (len - 1 < 2^24 is exact).
 __device__ __forceinline__ int cell_index(float t, int len)
 {
-    if(!(t >= 0.0f)) return 0;
-    if(t >= (float)len) return len - 1;
-    int i = (int)t;
-    return i > len - 1 ? len - 1 : i;
+    return (int)fminf(fmaxf(t, 0.0f), (float)(len - 1));
 }
 
 struct CellIds {
@@ -250,7 +251,7 @@ struct StepCells {
 
 __device__ __forceinline__ StepCells start_cells(const QueryParams& P, float x, float y, float z)
 {
-    return {grid_cell(P, x), grid_cell(P, y), grid_cell(P, z), !(isnan(x) || isnan(y) || isnan(z))};
+    return {grid_cell(P, x), grid_cell(P, y), grid_cell(P, z), (x == x) & (y == y) & (z == z)};
 }
 
 // true when the step box [a, b] (per-axis min/max) hits no obstacle.  The grid
@@ -266,6 +267,9 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
     const float lx = ax > bx ? bx : ax, hx = ax > bx ? ax : bx;
     const float ly = ay > by ? by : ay, hy = ay > by ? ay : by;
     const float lz = az > bz ? bz : az, hz = az > bz ? az : bz;
+    // loops stop at the first hit (a flag, not a return from inside them:
+    // fewer divergent exits for the compiler to reconverge every step)
+    bool hit = false;
     if(grid.start != nullptr)
         {
             const StepCells a = sc;
@@ -273,38 +277,41 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
             const int x0 = min(a.x, sc.x), x1 = max(a.x, sc.x);
             const int y0 = min(a.y, sc.y), y1 = max(a.y, sc.y);
             const int z0 = min(a.z, sc.z), z1 = max(a.z, sc.z);
-            const uint32_t n_cells = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1));
-            if(a.ok && sc.ok && n_cells <= kGridMaxVisit)
+            const int G = (int)P.grid_dim;
+            // cell coordinates are clamped to [0, G), so both loads stay in bounds
+            const int c0 = (x0 * G + y0) * G + z0;
+            uint32_t j = grid.start[c0];
+            const uint32_t e0 = grid.start[c0 + 1];
+            const bool cells_ok = a.ok & sc.ok;
+            if(cells_ok & (x0 == x1) & (y0 == y1) & (z0 == z1))
                 {
-                    const int G = (int)P.grid_dim;
-                    if(n_cells == 1)
+                    // the common case: both end points in one cell
+                    for(; j < e0 && !hit; ++j)
                         {
-                            // the common case: both end points in one cell
-                            const int c = (x0 * G + y0) * G + z0;
-                            const uint32_t e = grid.start[c + 1];
-                            for(uint32_t j = grid.start[c]; j < e; ++j)
-                                {
-                                    ++cnt.tests;
-                                    if(PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
-                                }
-                            return true;
+                            ++cnt.tests;
+                            hit = PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz);
                         }
-                    for(int cx = x0; cx <= x1; ++cx)
-                        for(int cy = y0; cy <= y1; ++cy)
-                            for(int cz = z0; cz <= z1; ++cz)
+                    return !hit;
+                }
+            const uint32_t n_cells = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1));
+            if(cells_ok & (n_cells <= kGridMaxVisit))
+                {
+                    for(int cx = x0; cx <= x1 && !hit; ++cx)
+                        for(int cy = y0; cy <= y1 && !hit; ++cy)
+                            for(int cz = z0; cz <= z1 && !hit; ++cz)
                                 {
                                     const int c = (cx * G + cy) * G + cz;
                                     const uint32_t e = grid.start[c + 1];
-                                    for(uint32_t j = grid.start[c]; j < e; ++j)
+                                    for(uint32_t k = grid.start[c]; k < e && !hit; ++k)
                                         {
                                             ++cnt.tests;
-                                            if(PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz)) return false;
+                                            hit = PLANAR ? box_hit_xy(obs, grid_item(grid, k), lx, ly, hx, hy)
+                                                         : box_hit(obs, grid_item(grid, k), lx, ly, lz, hx, hy, hz);
                                         }
                                 }
-                    return true;
+                    return !hit;
                 }
         }
-    bool hit = false;
     for(uint32_t o = 0; o < n_obs; ++o) hit |= PLANAR ? box_hit_xy(obs, o, lx, ly, hx, hy) : box_hit(obs, o, lx, ly, lz, hx, hy, hz);
     cnt.tests += n_obs;
     return !hit;
