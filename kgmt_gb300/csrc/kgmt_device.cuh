@@ -363,27 +363,38 @@ __device__ __forceinline__ bool propagate_di(const QueryParams& P, const GridVie
                     float sum = ref_rule ? v[d] + ((v[d] + 2.0f * half) + full) : ((v[d] + 2.0f * half) + 2.0f * half) + full;
                     x[d] = sum * h;
                 }
-            if(div6_exact(x[0]) && div6_exact(x[1]) && div6_exact(x[2]))
-                {
+            // one rarely-taken branch per step covers both the exact-division
+            // fallback and the bound checks
+            const bool exact = div6_exact(x[0]) & div6_exact(x[1]) & div6_exact(x[2]);
+            float pn[3];
 #pragma unroll
-                    for(int d = 0; d < 3; ++d) p[d] = p[d] + div6_fast(x[d]);
-                }
-            else
-                {
-#pragma unroll
-                    for(int d = 0; d < 3; ++d) p[d] = p[d] + x[d] / 6.0f;
-                }
+            for(int d = 0; d < 3; ++d) pn[d] = p[d] + div6_fast(x[d]);
 #pragma unroll
             for(int d = 0; d < 3; ++d) v[d] = v[d] + dv[d];
             // velocity bound, then workspace bound: either ends the sample here
-            const bool out = (v[0] < P.v_min) | (v[0] > P.v_max) | (v[1] < P.v_min) | (v[1] > P.v_max) | (v[2] < P.v_min) |
-                             (v[2] > P.v_max) | (p[0] < P.ws_min) | (p[0] > P.ws_max) | (p[1] < P.ws_min) | (p[1] > P.ws_max) |
-                             (p[2] < P.ws_min) | (p[2] > P.ws_max);
-            if(out)
+            bool out = (v[0] < P.v_min) | (v[0] > P.v_max) | (v[1] < P.v_min) | (v[1] > P.v_max) | (v[2] < P.v_min) | (v[2] > P.v_max) |
+                       (pn[0] < P.ws_min) | (pn[0] > P.ws_max) | (pn[1] < P.ws_min) | (pn[1] > P.ws_max) | (pn[2] < P.ws_min) |
+                       (pn[2] > P.ws_max);
+            if(!exact | out)
                 {
-                    ok = false;
-                    break;
+                    if(!exact)
+                        {
+#pragma unroll
+                            for(int d = 0; d < 3; ++d) pn[d] = p[d] + x[d] / 6.0f;
+                            out = (v[0] < P.v_min) | (v[0] > P.v_max) | (v[1] < P.v_min) | (v[1] > P.v_max) | (v[2] < P.v_min) |
+                                  (v[2] > P.v_max) | (pn[0] < P.ws_min) | (pn[0] > P.ws_max) | (pn[1] < P.ws_min) | (pn[1] > P.ws_max) |
+                                  (pn[2] < P.ws_min) | (pn[2] > P.ws_max);
+                        }
+                    if(out)
+                        {
+#pragma unroll
+                            for(int d = 0; d < 3; ++d) p[d] = pn[d];
+                            ok = false;
+                            break;
+                        }
                 }
+#pragma unroll
+            for(int d = 0; d < 3; ++d) p[d] = pn[d];
             if(!step_free(P, grid, obs, n_obs, q0, q1, q2, p[0], p[1], p[2], sc, cnt))
                 {
                     ok = false;

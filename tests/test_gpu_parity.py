@@ -101,6 +101,27 @@ def test_propagate_di_bit_exact_vs_oracle(rule):
     assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
 
 
+@pytest.mark.parametrize("rule", [0, 1])
+def test_propagate_di_exact_division_fallback(rule):
+    """Samples whose RK4 increments are zero or below 2^-98 in magnitude take
+    the true-division branch of the step (the fused multiply-add form of x / 6
+    is exact only above that): zero acceleration (u = 0.5 on [-1, 1]) with zero
+    or tiny velocities, and signed zeros."""
+    q = W.double_integrator_query(seed=2)
+    cfg = q.config.replace(di_rule=rule)
+    x0, u = random_inputs(cfg, 256, 17)
+    u[:, 0:3] = 0.5
+    x0[:64, 3:6] = 0.0
+    x0[64:96, 3:6] = -0.0
+    x0[96:160, 3:6] = np.float32(1e-33) * np.sign(x0[96:160, 3:6] + 1e-30)
+    x0[160:192, 3:6] = np.float32(2.0 ** -140)  # subnormal velocities
+    gx, gv, g1, g2 = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, o1, o2 = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert np.array_equal(gv, ov)
+    assert np.array_equal(gx.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
+
+
 def test_propagate_quad_bit_exact_vs_oracle():
     q = W.quadrotor_query(seed=2)
     cfg = q.config
