@@ -129,6 +129,18 @@ class ClockSampler:
                 "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
 
 
+# DRAM bytes (read + write) per k_propagate launch on this workload, from one
+# ncu capture of a planning step (dram__bytes_read.sum + dram__bytes_write.sum
+# summed over its 132 propagate launches, --cache-control none --clock-control
+# none): 462 MB read + 1992 MB written.  The live algorithmic bytes per launch
+# (sample rows, parent, region and flag written; parent rows and frontier
+# indices read) are reported beside it.
+PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (461.74e6 + 1992.33e6) / 132
+# algorithmic bytes per double-integrator sample: row (10 floats), parent,
+# region and flag written; the parent's row and its frontier index read
+PROPAGATE_BYTES_PER_SAMPLE = 10 * 4 + 4 + 4 + 1 + 10 * 4 + 4
+
+
 # ---------------------------------------------------------------------------
 # FP32 denominator of the propagate roofline
 # ---------------------------------------------------------------------------
@@ -352,7 +364,11 @@ def run_ours(args) -> None:
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": {"kernel": "k_propagate", "bound": "fp32", "achieved": achieved * 1e-12, "peak": fp32_peak * 1e-12,
-                         "unit": "T FP32 lane-ops/s", "frac": achieved / fp32_peak, "traffic": None,
+                         "unit": "T FP32 lane-ops/s", "frac": achieved / fp32_peak,
+                         "traffic": PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH,
+                         "traffic_unit": "DRAM bytes per launch (ncu capture of this workload)",
+                         "algorithmic_bytes_per_launch": st["samples"] * PROPAGATE_BYTES_PER_SAMPLE
+                         / max(1, st["launches_propagate"]),
                          "peak_source": "measured: cuBLAS SGEMM 8192^3 (TF32 off) FLOP/s / 2",
                          "avg_launch_ms": prop_ms_avg, "launches": st["launches_propagate"],
                          "share_of_kernel_time": st["ms_propagate"] / max(1e-9, total_kernel_ms)},
