@@ -1018,12 +1018,12 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             if(lt < n_old)
                 {
                     // ---- re-activation of old nodes (KGMT.cu:364-377) ----
-                    const uint32_t i0 = lt * kTileC + threadIdx.x * 4;
+                    const uint32_t i0 = lt * kTileC + threadIdx.x * kAppendPer;
                     const float fa = s_fa;
                     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
                     uint32_t flags = 0, cnt = 0;
 #pragma unroll
-                    for(int j = 0; j < 4; ++j)
+                    for(int j = 0; j < kAppendPer; ++j)
                         {
                             const uint32_t i = i0 + j;
                             if(i < tree_size)
@@ -1044,26 +1044,37 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     __syncthreads();
                     uint32_t pos = (uint32_t)s_prefix + excl;
 #pragma unroll
-                    for(int j = 0; j < 4; ++j)
+                    for(int j = 0; j < kAppendPer; ++j)
                         if(flags & (1u << j)) p.rep_old[pos++] = i0 + j;
                 }
             else
                 {
                     // ---- ordered append of accepted samples (KGMT.cu:317-362) ----
                     const uint32_t lts = lt - n_old;
-                    const uint32_t s0 = lts * kTileC + threadIdx.x * 4;
+                    const uint32_t s0 = lts * kTileC + threadIdx.x * kAppendPer;
                     const uint32_t ns = st.n_samples;
                     uint32_t acc_bits = 0, ca = 0, cw = 0;
-                    uint32_t w[4] = {0, 0, 0, 0};
+                    // flags and regions are read together, then the accepted
+                    // samples' valid counts: two round trips, not three
+                    uint32_t fl[kAppendPer];
+                    int32_t rg[kAppendPer];
 #pragma unroll
-                    for(int j = 0; j < 4; ++j)
+                    for(int j = 0; j < kAppendPer; ++j)
                         {
                             const uint32_t s = s0 + j;
-                            if(s < ns && p.uflag[s])
+                            fl[j] = s < ns ? p.uflag[s] : 0u;
+                            rg[j] = s < ns ? p.ur1[s] : 0;
+                        }
+                    uint32_t w[kAppendPer];
+#pragma unroll
+                    for(int j = 0; j < kAppendPer; ++j)
+                        {
+                            w[j] = 0;
+                            if(fl[j])
                                 {
                                     acc_bits |= 1u << j;
                                     ++ca;
-                                    w[j] = p.valid[p.ur1[s]] < kSparseValidLimit ? kRepeatSparse : kRepeatDense;
+                                    w[j] = p.valid[rg[j]] < kSparseValidLimit ? kRepeatSparse : kRepeatDense;
                                     cw += w[j];
                                 }
                         }
@@ -1083,14 +1094,14 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     uint32_t iw = (uint32_t)(pre & 0xffffffffull) + (excl & 0xffffu);
                     const int D = (int)p.sample_dim;
 #pragma unroll
-                    for(int j = 0; j < 4; ++j)
+                    for(int j = 0; j < kAppendPer; ++j)
                         {
                             if(!(acc_bits & (1u << j))) continue;
                             const uint32_t s = s0 + j;
                             const uint32_t idx = ia++;
                             // everything the sample needs is loaded before its
                             // first store (one round trip, not one per field)
-                            const int32_t par = __ldg(p.up + s), r1 = __ldg(p.ur1 + s);
+                            const int32_t par = __ldg(p.up + s), r1 = rg[j];
                             const float dist = append_row(p, p.us + (size_t)s * D, p.tree + (size_t)idx * D, D);
                             p.parent[idx] = par;
                             p.cost[idx] = dist;

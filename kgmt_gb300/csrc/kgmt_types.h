@@ -16,7 +16,8 @@ namespace kgmt {
 constexpr int kMaxSampleDim = KGMT_MAX_SAMPLE_DIM;
 constexpr int kScoreLanes = 256;        // fixed summation shape of the score total
 constexpr int kTileC = 1024;            // elements per append / re-activation tile
-constexpr int kAppendThreads = 256;     // threads per append block (4 elements each)
+constexpr int kAppendThreads = 256;     // threads per append block
+constexpr int kAppendPer = kTileC / kAppendThreads;  // elements per append thread
 constexpr int kRootRepeat = 5;          // KGMT.cu:67
 constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
 constexpr int kRepeatDense = 1;         // KGMT.cu:338-339
