@@ -659,11 +659,15 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
 {
     const float F = (float)p.fine_cells;
     constexpr int U = 4;  // regions whose loads are issued together
+    // the thread's first U regions keep their raw score in registers for the
+    // normalisation pass (no re-read of what it just wrote)
+    float kept[U];
     for(int l = threadIdx.x; l < kScoreLanes; l += NT)
         {
             float acc = 0.0f;
             for(uint32_t r0 = (uint32_t)l; r0 < p.regions; r0 += U * kScoreLanes)
                 {
+                    const bool first = l == (int)threadIdx.x && r0 == (uint32_t)l;
                     uint64_t m[U];
                     int32_t nv[U], n[U];
 #pragma unroll
@@ -701,6 +705,7 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
                                     keep = raw;
                                 }
                             p.score[r] = keep;
+                            if(first) kept[k] = keep;
                             acc = acc + raw;
                         }
                 }
@@ -713,14 +718,20 @@ __device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes
             __syncthreads();
         }
     const float total = lanes[0];
-    // each lane re-reads only what it wrote itself (raw score, -1 for regions
-    // without valid samples)
+    // raw score (-1 for regions without valid samples) -> normalised score;
+    // past the registers each lane re-reads only what it wrote itself
+    auto norm = [&](float raw) { return raw < 0.0f ? 1.0f : (total > 0.0f ? p.epsilon + raw / total : p.epsilon); };
     for(int l = threadIdx.x; l < kScoreLanes; l += NT)
-        for(uint32_t r = (uint32_t)l; r < p.regions; r += kScoreLanes)
-            {
-                const float raw = p.score[r];
-                p.score[r] = raw < 0.0f ? 1.0f : (total > 0.0f ? p.epsilon + raw / total : p.epsilon);
-            }
+        {
+            uint32_t r = (uint32_t)l;
+            if(l == (int)threadIdx.x)
+                {
+#pragma unroll
+                    for(int k = 0; k < U; ++k, r += kScoreLanes)
+                        if(r < p.regions) p.score[r] = norm(kept[k]);
+                }
+            for(; r < p.regions; r += kScoreLanes) p.score[r] = norm(p.score[r]);
+        }
     if(threadIdx.x == 0) st.score_total = total;
 }
 
