@@ -260,7 +260,7 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
                         {
                             const uint32_t ns = __ldcg(&S[q].n_samples);
                             ta = (ns + prop_tile - 1) / prop_tile;
-                            told = (__ldcg(&S[q].tree_size) + kTileC - 1) / kTileC;
+                            told = (__ldcg(&S[q].tree_size) + kTileOld - 1) / kTileOld;
                             tc = told + (ns + kTileC - 1) / kTileC;
                             run = 1;
                         }
@@ -305,7 +305,7 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
                 {
                     uint32_t ns = __ldcg(&S[q].n_samples);
                     ta = (ns + prop_tile - 1) / prop_tile;
-                    told = (__ldcg(&S[q].tree_size) + kTileC - 1) / kTileC;
+                    told = (__ldcg(&S[q].tree_size) + kTileOld - 1) / kTileOld;
                     tc = told + (ns + kTileC - 1) / kTileC;
                     run = 1;
                 }
@@ -1029,19 +1029,38 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             if(lt < n_old)
                 {
                     // ---- re-activation of old nodes (KGMT.cu:364-377) ----
-                    const uint32_t i0 = lt * kTileC + threadIdx.x * kAppendPer;
+                    const uint32_t i0 = lt * kTileOld + threadIdx.x * kOldPer;
                     const float fa = s_fa;
                     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
                     uint32_t flags = 0, cnt = 0;
+                    // node regions four at a time (i0 is a multiple of 4: the
+                    // 16-byte loads are aligned), then the region scores
+                    static_assert(kOldPer % 4 == 0 && kOldPer <= 32, "re-activation: 4-node loads, one flag bit per node");
+                    int32_t reg[kOldPer];
 #pragma unroll
-                    for(int j = 0; j < kAppendPer; ++j)
+                    for(int g = 0; g < kOldPer; g += 4)
+                        {
+                            const uint32_t ib = i0 + g;
+                            if(ib + 3 < tree_size)
+                                {
+                                    const int4 v = *(const int4*)(p.node_r1 + ib);
+                                    reg[g] = v.x, reg[g + 1] = v.y, reg[g + 2] = v.z, reg[g + 3] = v.w;
+                                }
+                            else
+                                {
+#pragma unroll
+                                    for(int j = 0; j < 4; ++j) reg[g + j] = ib + j < tree_size ? p.node_r1[ib + j] : 0;
+                                }
+                        }
+#pragma unroll
+                    for(int j = 0; j < kOldPer; ++j)
                         {
                             const uint32_t i = i0 + j;
                             if(i < tree_size)
                                 {
                                     const U4 r = philox4x32_10(i, itr, 1u, 0u, k0, k1);
                                     const float ur = u01(r.x);
-                                    if(ur <= p.score[p.node_r1[i]] + fa)
+                                    if(ur <= p.score[reg[j]] + fa)
                                         {
                                             flags |= 1u << j;
                                             ++cnt;
@@ -1055,7 +1074,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     __syncthreads();
                     uint32_t pos = (uint32_t)s_prefix + excl;
 #pragma unroll
-                    for(int j = 0; j < kAppendPer; ++j)
+                    for(int j = 0; j < kOldPer; ++j)
                         if(flags & (1u << j)) p.rep_old[pos++] = i0 + j;
                 }
             else

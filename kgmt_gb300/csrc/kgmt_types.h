@@ -15,9 +15,13 @@ namespace kgmt {
 
 constexpr int kMaxSampleDim = KGMT_MAX_SAMPLE_DIM;
 constexpr int kScoreLanes = 256;        // fixed summation shape of the score total
-constexpr int kTileC = 1024;            // elements per append / re-activation tile
+constexpr int kTileC = 1024;            // samples per append tile
 constexpr int kAppendThreads = 256;     // threads per append block
-constexpr int kAppendPer = kTileC / kAppendThreads;  // elements per append thread
+constexpr int kAppendPer = kTileC / kAppendThreads;  // samples per append thread
+// old nodes per re-activation tile: larger than an append tile, so the fixed
+// latency of a tile (loads, scan, look-back, hand-over) covers more nodes
+constexpr int kTileOld = 4096;
+constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread
 constexpr int kRootRepeat = 5;          // KGMT.cu:67
 constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
 constexpr int kRepeatDense = 1;         // KGMT.cu:338-339
