@@ -406,6 +406,10 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     Sched s;
     std::memset(&s, 0, sizeof(s));
     s.prop_tile = block;
+    s.prop_block = block;
+    // two samples per thread once an iteration fills the resident threads of
+    // the double-integrator variant twice
+    s.pair_samples = 2u * (uint32_t)grid_a_[1] * block;
     s.host_running = d_running_;
     KGMT_CUDA(cudaMemcpyAsync(d_sched_, &s, sizeof(s), cudaMemcpyHostToDevice, stream_), "upload(sched)");
     KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");

@@ -247,14 +247,25 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
 {
     __shared__ uint32_t scratch[34];
     __shared__ uint32_t carry[3];
+    __shared__ uint32_t s_tile_size;
     const int n = (int)sched->n_slots;
-    const uint32_t prop_tile = sched->prop_tile;
+    const uint32_t block = sched->prop_block;
+    const uint32_t pair_samples = sched->pair_samples;
+    // samples of a running query, clamped so that sums over 32 or a block of
+    // slots cannot wrap (only the comparison with pair_samples matters)
+    auto samples_of = [&](int q) -> uint32_t {
+        if(q >= n || __ldcg(&S[q].status) != KGMT_QUERY_RUNNING) return 0u;
+        const uint32_t ns = __ldcg(&S[q].n_samples);
+        return ns < (1u << 22) ? ns : (1u << 22);
+    };
     if(n <= 32)
         {
             // up to 32 slots: one warp, shuffle scans, no block barriers but the last
             if(threadIdx.x < 32)
                 {
                     const int q = (int)threadIdx.x;
+                    const uint32_t total = __reduce_add_sync(0xffffffffu, samples_of(q));
+                    const uint32_t prop_tile = total >= pair_samples ? kPropPer * block : block;
                     uint32_t ta = 0, tc = 0, told = 0, run = 0;
                     if(q < n && __ldcg(&S[q].status) == KGMT_QUERY_RUNNING)
                         {
@@ -287,6 +298,7 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
                             sched->tiles_c = ic;
                             sched->running = ir;
                             sched->ticket_a = 0;
+                            sched->prop_tile = prop_tile;
                             if(ir) sched->iterations += 1;
                             if(sched->host_running) *(volatile uint32_t*)sched->host_running = ir;
                         }
@@ -294,8 +306,21 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
             __syncthreads();
             return;
         }
+    {
+        // this iteration's propagate tile size from all running queries' samples
+        uint32_t mine = 0;
+        for(int q = threadIdx.x; q < n; q += blockDim.x)
+            {
+                mine += samples_of(q);
+                if(mine >= pair_samples) mine = pair_samples;
+            }
+        uint32_t total;
+        block_exclusive_scan<kAppendThreads>(mine, scratch, &total);
+        if(threadIdx.x == 0) s_tile_size = total >= pair_samples ? kPropPer * block : block;
+    }
     if(threadIdx.x == 0) carry[0] = carry[1] = carry[2] = 0;
     __syncthreads();
+    const uint32_t prop_tile = s_tile_size;
     for(int base = 0; base < n; base += blockDim.x)
         {
             int q = base + threadIdx.x;
@@ -336,6 +361,7 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
             sched->tiles_c = carry[1];
             sched->running = carry[2];
             sched->ticket_a = 0;
+            sched->prop_tile = prop_tile;
             if(carry[2]) sched->iterations += 1;
             if(sched->host_running) *(volatile uint32_t*)sched->host_running = carry[2];
         }
@@ -756,7 +782,7 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
     __shared__ float s_lanes[kScoreLanes];
     __shared__ uint32_t s_base[kBaseCache];
     __shared__ uint32_t s_hist[kSortBins];
-    __shared__ uint32_t s_perm[NT];
+    __shared__ uint32_t s_perm[kPropPer * NT];
     __shared__ int s_tile, s_q, s_last;
     if(blockIdx.x == 0 && threadIdx.x == 0)
         {
@@ -766,6 +792,8 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
         }
     const uint32_t total = sched->tiles_a;
     const int n_slots = (int)sched->n_slots;
+    // samples per thread this iteration (the schedule sized the tiles)
+    const int per = sched->prop_tile > (uint32_t)NT ? kPropPer : 1;
     if(blockIdx.x >= total) return;
     if(threadIdx.x == 0)
         {
@@ -832,20 +860,30 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                 }
             const uint32_t lt = t - bases.base[q];
             const int model = s_p.model;
-            // counting sort of the tile's samples by step count (dead lanes
-            // last): thread i then takes the i-th sample in that order
+            // counting sort of the tile's kPropPer * NT samples by step count
+            // (dead lanes last); pass 0 gives thread i the i-th shortest, pass
+            // 1 the i-th longest, so every thread gets about the same work
+            // and a warp's lanes loop about equally long in each pass
             {
-                const uint32_t s0 = lt * NT + threadIdx.x;
-                int key = kSortBins - 1;
-                if(s0 < s_c.n_samples)
-                    {
-                        int k = 1;
-                        with_model<MODELS>(model, [&](auto m) { k = sample_steps<decltype(m)::value>(s_p, s_c, s0); });
-                        key = k < kSortBins - 1 ? k : kSortBins - 2;
-                    }
+                uint32_t s0[kPropPer], rank[kPropPer];
+                int key[kPropPer];
                 if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = 0;
+#pragma unroll
+                for(int h = 0; h < kPropPer; ++h)
+                    {
+                        // with one sample per thread the second key is a dead lane
+                        s0[h] = h < per ? (lt * per + h) * NT + threadIdx.x : 0xFFFFFFFFu;
+                        key[h] = kSortBins - 1;
+                        if(s0[h] < s_c.n_samples)
+                            {
+                                int k = 1;
+                                with_model<MODELS>(model, [&](auto m) { k = sample_steps<decltype(m)::value>(s_p, s_c, s0[h]); });
+                                key[h] = k < kSortBins - 1 ? k : kSortBins - 2;
+                            }
+                    }
                 __syncthreads();
-                const uint32_t rank = atomicAdd(&s_hist[key], 1u);
+#pragma unroll
+                for(int h = 0; h < kPropPer; ++h) rank[h] = atomicAdd(&s_hist[key[h]], 1u);
                 __syncthreads();
                 if(threadIdx.x < 32)
                     {
@@ -861,31 +899,37 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                         if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = x - v;
                     }
                 __syncthreads();
-                s_perm[s_hist[key] + rank] = s0;
+#pragma unroll
+                for(int h = 0; h < kPropPer; ++h) s_perm[s_hist[key[h]] + rank[h]] = s0[h];
                 __syncthreads();
             }
-            const uint32_t s = s_perm[threadIdx.x];
-            const bool live = s < s_c.n_samples;
             const float4* obs = s_p.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : s_p.obstacles;
-            float x0[KGMT_MAX_SAMPLE_DIM], u[8];
-            uint32_t par = 0;
-            if(live)
+            static_assert(kPropPer == 2, "the passes pair the i-th shortest with the i-th longest sample");
+            for(int pass = 0; pass < per; ++pass)
                 {
-                    with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(s_p, s_c, s, x0, u); });
+                    // pass 0: the i-th shortest; pass 1: the i-th longest
+                    const uint32_t s = s_perm[pass == 0 ? threadIdx.x : (uint32_t)(2 * NT - 1) - threadIdx.x];
+                    const bool live = s < s_c.n_samples;
+                    float x0[KGMT_MAX_SAMPLE_DIM], u[8];
+                    uint32_t par = 0;
+                    if(live)
+                        {
+                            with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(s_p, s_c, s, x0, u); });
+                        }
+                    if(pass == 0 && wait_obs)
+                        {
+                            uint32_t spins = 0;
+                            while(!mbar_try_wait(&bar, phase))
+                                if(++spins > kSpinLimit)
+                                    {
+                                        if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
+                                        break;
+                                    }
+                            phase ^= 1u;
+                        }
+                    const GridView grid{(s_p.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, s_p.grid_items};
+                    with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh); });
                 }
-            if(wait_obs)
-                {
-                    uint32_t spins = 0;
-                    while(!mbar_try_wait(&bar, phase))
-                        if(++spins > kSpinLimit)
-                            {
-                                if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
-                                break;
-                            }
-                    phase ^= 1u;
-                }
-            const GridView grid{(s_p.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, s_p.grid_items};
-            with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh); });
             __syncthreads();
             if(threadIdx.x == 0)
                 {

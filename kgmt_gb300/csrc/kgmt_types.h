@@ -22,6 +22,12 @@ constexpr int kAppendPer = kTileC / kAppendThreads;  // samples per append threa
 // latency of a tile (loads, scan, look-back, hand-over) covers more nodes
 constexpr int kTileOld = 4096;
 constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread
+// samples per propagate thread and tile in iterations with enough samples to
+// fill the resident threads twice: a tile of kPropPer * NT samples is sorted
+// by step count and thread t runs the t-th shortest and the t-th longest, so
+// the threads of a block finish together.  Smaller iterations keep one sample
+// per thread (more tiles in parallel, a shorter chain per thread).
+constexpr int kPropPer = 2;
 constexpr int kRootRepeat = 5;          // KGMT.cu:67
 constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
 constexpr int kRepeatDense = 1;         // KGMT.cu:338-339
@@ -164,7 +170,9 @@ struct Sched {
     uint32_t finalized;
     uint32_t error;
     uint32_t iterations;  // engine iterations launched with work
-    uint32_t prop_tile;   // samples per propagate tile (= propagate block size)
+    uint32_t prop_tile;   // samples per propagate tile this iteration: prop_block, or kPropPer x prop_block
+    uint32_t prop_block;  // propagate block size
+    uint32_t pair_samples;  // iterations with at least this many samples use kPropPer samples per thread
     // mapped pinned host word that mirrors `running` (or null): the host polls
     // it without a copy in the stream between graph replays
     uint32_t* host_running;
