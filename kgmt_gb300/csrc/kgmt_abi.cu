@@ -215,9 +215,8 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
     CHECK_ST(p->eng.admit(0, 1, 1));
     CHECK_ST(p->eng.run_until_done(p->cfg.max_iterations));
     CHECK_ST(p->eng.extract_paths(1));
-    CHECK_ST(p->eng.read_states(0, 1, &p->state));
     uint32_t err = 0;
-    CHECK_ST(p->eng.read_error(&err));
+    CHECK_ST(p->eng.read_states_and_error(0, 1, &p->state, &err));
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "kgmt_plan: a device-side wait gave up (error bits " + std::to_string(err) + ")");
     p->planned = true;
     return KGMT_OK;
@@ -374,9 +373,8 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     CHECK_ST(b->eng.run_until_done(max_iters));
     CHECK_ST(b->eng.extract_paths(n));
     b->states.resize(n);
-    CHECK_ST(b->eng.read_states(0, n, b->states.data()));
     uint32_t err = 0;
-    CHECK_ST(b->eng.read_error(&err));
+    CHECK_ST(b->eng.read_states_and_error(0, n, b->states.data(), &err));
     b->n_last = n;
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "batch: a device-side wait gave up (error bits " + std::to_string(err) + ")");
     // counters of this call

@@ -319,6 +319,8 @@ kgmt_result to_result(const QueryState& s, uint64_t ticket)
 // ---------------------------------------------------------------------------
 // engine
 // ---------------------------------------------------------------------------
+__global__ void k_set_n_slots(Sched* sched, uint32_t n) { sched->n_slots = n; }
+
 __global__ void k_set_endpoints(QueryParams* P, uint32_t first, uint32_t count, const float* __restrict__ inits,
                                 const float* __restrict__ goals)
 {
@@ -335,6 +337,7 @@ Engine::~Engine()
     for(auto& e : ev_)
         if(e) cudaEventDestroy(e);
     if(h_running_) cudaFreeHost(h_running_);
+    if(h_stage_states_) cudaFreeHost(h_stage_states_);
     cudaFree(d_params_);
     cudaFree(d_states_);
     cudaFree(d_sched_);
@@ -386,6 +389,7 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     // the running count, written by the device into mapped pinned memory
     KGMT_CUDA(cudaHostAlloc((void**)&h_running_, sizeof(uint32_t) * 2, cudaHostAllocMapped), "cudaHostAlloc(mapped)");
     KGMT_CUDA(cudaHostGetDevicePointer((void**)&d_running_, h_running_, 0), "cudaHostGetDevicePointer");
+    KGMT_CUDA(cudaMallocHost((void**)&h_stage_states_, sizeof(QueryState) * slots), "cudaMallocHost(states)");
     for(auto& e : ev_) KGMT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
     return set_prop_block(prop_block ? prop_block : 256);
 }
@@ -473,9 +477,10 @@ kgmt_status Engine::set_active(uint32_t n_active)
             set_error("set_active: more slots than the engine holds");
             return KGMT_ERR_INVALID_ARG;
         }
-    KGMT_CUDA(cudaMemcpyAsync(&d_sched_->n_slots, &n_active, sizeof(uint32_t), cudaMemcpyHostToDevice, stream_), "upload(n_slots)");
-    // n_active lives on the host stack: wait for the copy
-    KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");
+    // by value through a kernel parameter: no host memory to keep alive, no wait
+    k_set_n_slots<<<1, 1, 0, stream_>>>(d_sched_, n_active);
+    KGMT_CUDA(cudaGetLastError(), "k_set_n_slots");
+    launches_ += 1;
     return KGMT_OK;
 }
 
@@ -638,6 +643,25 @@ kgmt_status Engine::read_states(uint32_t first, uint32_t count, QueryState* out)
     if(count == 0) return KGMT_OK;
     KGMT_CUDA(cudaMemcpyAsync(out, d_states_ + first, sizeof(QueryState) * count, cudaMemcpyDeviceToHost, stream_), "download(states)");
     KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::read_states_and_error(uint32_t first, uint32_t count, QueryState* out, uint32_t* err)
+{
+    // both copies land in pinned staging, so they are queued together and
+    // waited for once (a pageable destination would wait for each copy)
+    if(first + count > slots_)
+        {
+            set_error("read_states_and_error: slot range out of bounds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    if(count)
+        KGMT_CUDA(cudaMemcpyAsync(h_stage_states_, d_states_ + first, sizeof(QueryState) * count, cudaMemcpyDeviceToHost, stream_),
+                  "download(states)");
+    KGMT_CUDA(cudaMemcpyAsync(&h_running_[1], &d_sched_->error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "download(error)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    if(count) std::memcpy(out, h_stage_states_, sizeof(QueryState) * count);
+    *err = h_running_[1];
     return KGMT_OK;
 }
 

@@ -86,6 +86,8 @@ class Engine {
     // runs exactly `iters` iterations (served loop)
     kgmt_status run_iterations(uint32_t iters);
     kgmt_status read_states(uint32_t first, uint32_t count, QueryState* out);
+    // states and the error bits in one wait
+    kgmt_status read_states_and_error(uint32_t first, uint32_t count, QueryState* out, uint32_t* err);
     kgmt_status extract_paths(uint32_t n_active);
     kgmt_status read_error(uint32_t* err);
     kgmt_status set_prop_block(uint32_t block);
@@ -132,7 +134,8 @@ class Engine {
     uint32_t* d_tile_a_ = nullptr;
     uint32_t* d_tile_c_ = nullptr;
     uint32_t* d_tile_old_ = nullptr;
-    uint32_t* h_running_ = nullptr;  // mapped pinned host word the device writes (Sched::host_running)
+    uint32_t* h_running_ = nullptr;  // mapped pinned host words: [0] Sched::host_running, [1] error readback
+    QueryState* h_stage_states_ = nullptr;  // pinned staging for state readbacks
     uint32_t* d_running_ = nullptr;  // its device address
     cudaEvent_t ev_[2] = {nullptr, nullptr};
     cudaGraphExec_t graph_ = nullptr;
