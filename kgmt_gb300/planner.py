@@ -138,12 +138,16 @@ class BatchPlanner:
         except Exception:
             pass
 
-    def plan(self, cfgs, inits, goals, obstacles, obs_offset, obs_count) -> list[dict]:
+    def plan(self, cfgs, inits, goals, obstacles, obs_offset, obs_count, carr=None, res=None):
         """Host arrays: inits / goals [n][17], obstacles [m][6], offsets and
-        counts in boxes.  Returns one result dict per query."""
+        counts in boxes.  Returns one result dict per query, or -- when the
+        caller passes its own result array `res` (and, to skip repacking,
+        the configs packed once with pack_configs as `carr`) -- fills `res`
+        and returns it."""
         n = len(cfgs)
-        carr = pack_configs(cfgs)
-        res = (KgmtResult * n)()
+        raw = res is not None
+        carr = pack_configs(cfgs) if carr is None else carr
+        res = (KgmtResult * n)() if res is None else res
         inits, goals, obstacles = _f32(inits), _f32(goals), _f32(obstacles)
         off = np.ascontiguousarray(obs_offset, np.uint32)
         cnt = np.ascontiguousarray(obs_count, np.uint32)
@@ -151,7 +155,7 @@ class BatchPlanner:
                                         off.ctypes.data, cnt.ctypes.data, res))
         self._n = n
         self._cfgs = list(cfgs)
-        return [r.as_dict() for r in res]
+        return res if raw else [r.as_dict() for r in res]
 
     def plan_device(self, cfgs, d_inits, d_goals, d_obstacles, obs_offset, obs_count, carr=None, res=None):
         """Inputs already on the device (torch tensors or addresses)."""
