@@ -414,6 +414,8 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     // two samples per thread once an iteration fills the resident threads of
     // the double-integrator variant twice
     s.pair_samples = 2u * (uint32_t)grid_a_[1] * block;
+    s.n_sms = (uint32_t)sms;
+    s.old_tile = kTileOld;
     s.host_running = d_running_;
     KGMT_CUDA(cudaMemcpyAsync(d_sched_, &s, sizeof(s), cudaMemcpyHostToDevice, stream_), "upload(sched)");
     KGMT_CUDA(cudaStreamSynchronize(stream_), "sync");

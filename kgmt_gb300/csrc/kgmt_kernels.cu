@@ -31,134 +31,9 @@
 #include <climits>
 #include <type_traits>
 
-#include "kgmt_device.cuh"
-#include "kgmt_kernels.h"
+#include "kgmt_iter.cuh"
 
 namespace kgmt {
-
-// ---------------------------------------------------------------------------
-// small device helpers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-    return ok != 0;
-}
-
-// bulk global -> shared copy through the TMA engine; bytes % 16 == 0, both
-// addresses 16-byte aligned
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ unsigned long long globaltimer()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p)
-{
-    return *(const volatile unsigned long long*)p;
-}
-
-__device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned long long v)
-{
-    *(volatile unsigned long long*)p = v;
-}
-
-// Tile bases of up to kBaseCache slots are copied to shared memory once per
-// block, so finding a tile's query is a binary search in shared memory
-// instead of ~log2(slots) dependent global loads.
-constexpr int kBaseCache = 2048;
-
-struct BaseCache {
-    const uint32_t* base;  // shared copy, or the global array when too many slots
-    int n;
-};
-
-__device__ __forceinline__ BaseCache cache_bases(const uint32_t* __restrict__ g, int n, uint32_t* s)
-{
-    if(n + 1 > kBaseCache) return {g, n};
-    for(int i = threadIdx.x; i <= n; i += blockDim.x) s[i] = g[i];
-    __syncthreads();
-    return {s, n};
-}
-
-// last slot q with base[q] <= t (base is an exclusive prefix over n slots,
-// base[n] = total, t < total)
-__device__ __forceinline__ int find_slot(const uint32_t* __restrict__ base, int n, uint32_t t)
-{
-    int lo = 0, hi = n;
-    while(lo < hi)
-        {
-            int mid = (lo + hi + 1) >> 1;
-            if(base[mid] <= t) lo = mid;
-            else hi = mid - 1;
-        }
-    return lo;
-}
-
-// block-wide exclusive scan of one uint32 per thread; returns the exclusive
-// prefix, *total the block sum.  scratch: >= 33 words of shared memory.
-template <int NT>
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* scratch, uint32_t* total)
-{
-    constexpr int NW = NT / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for(int o = 1; o < 32; o <<= 1)
-        {
-            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if(lane >= o) x += y;
-        }
-    if(lane == 31) scratch[warp] = x;
-    __syncthreads();
-    if(warp == 0)
-        {
-            uint32_t w = lane < NW ? scratch[lane] : 0u;
-            uint32_t z = w;
-#pragma unroll
-            for(int o = 1; o < 32; o <<= 1)
-                {
-                    uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
-                    if(lane >= o) z += y;
-                }
-            if(lane < NW) scratch[lane] = z - w;
-            if(lane == NW - 1) scratch[32] = z;
-        }
-    __syncthreads();
-    uint32_t excl = scratch[warp] + x - v;
-    *total = scratch[32];
-    __syncthreads();
-    return excl;
-}
 
 // ---------------------------------------------------------------------------
 // decoupled look-back over one chain of tiles of one query.  Word layout:
@@ -235,158 +110,6 @@ __device__ __forceinline__ void publish_and_lookback(unsigned long long* tiles, 
             st_volatile_u64(&tiles[lt], kStIncl | (prefix + agg));
             *s_prefix = prefix;
         }
-}
-
-// ---------------------------------------------------------------------------
-// schedule of the next iteration, computed by one block (the last query to
-// finalise, or the admission path): tiles per slot, prefix bases, running
-// count.  All threads of the calling block must enter.
-// ---------------------------------------------------------------------------
-__device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryState* __restrict__ S, Sched* sched, uint32_t* tile_a_base,
-                                 uint32_t* tile_c_base, uint32_t* tile_c_old)
-{
-    __shared__ uint32_t scratch[34];
-    __shared__ uint32_t carry[3];
-    __shared__ uint32_t s_tile_size;
-    const int n = (int)sched->n_slots;
-    const uint32_t block = sched->prop_block;
-    const uint32_t pair_samples = sched->pair_samples;
-    // samples of a running query, clamped so that sums over 32 or a block of
-    // slots cannot wrap (only the comparison with pair_samples matters)
-    auto samples_of = [&](int q) -> uint32_t {
-        if(q >= n || __ldcg(&S[q].status) != KGMT_QUERY_RUNNING) return 0u;
-        const uint32_t ns = __ldcg(&S[q].n_samples);
-        return ns < (1u << 22) ? ns : (1u << 22);
-    };
-    if(n <= 32)
-        {
-            // up to 32 slots: one warp, shuffle scans, no block barriers but the last
-            if(threadIdx.x < 32)
-                {
-                    const int q = (int)threadIdx.x;
-                    const uint32_t total = __reduce_add_sync(0xffffffffu, samples_of(q));
-                    const uint32_t prop_tile = total >= pair_samples ? kPropPer * block : block;
-                    uint32_t ta = 0, tc = 0, told = 0, run = 0;
-                    if(q < n && __ldcg(&S[q].status) == KGMT_QUERY_RUNNING)
-                        {
-                            const uint32_t ns = __ldcg(&S[q].n_samples);
-                            ta = (ns + prop_tile - 1) / prop_tile;
-                            told = (__ldcg(&S[q].tree_size) + kTileOld - 1) / kTileOld;
-                            tc = told + (ns + kTileC - 1) / kTileC;
-                            run = 1;
-                        }
-                    uint32_t ia = ta, ic = tc, ir = run;
-#pragma unroll
-                    for(int o = 1; o < 32; o <<= 1)
-                        {
-                            const uint32_t ya = __shfl_up_sync(0xffffffffu, ia, o);
-                            const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
-                            const uint32_t yr = __shfl_up_sync(0xffffffffu, ir, o);
-                            if(q >= o) ia += ya, ic += yc, ir += yr;
-                        }
-                    if(q < n)
-                        {
-                            tile_a_base[q] = ia - ta;
-                            tile_c_base[q] = ic - tc;
-                            tile_c_old[q] = told;
-                        }
-                    if(q == 31)
-                        {
-                            tile_a_base[n] = ia;
-                            tile_c_base[n] = ic;
-                            sched->tiles_a = ia;
-                            sched->tiles_c = ic;
-                            sched->running = ir;
-                            sched->ticket_a = 0;
-                            sched->prop_tile = prop_tile;
-                            if(ir) sched->iterations += 1;
-                            if(sched->host_running) *(volatile uint32_t*)sched->host_running = ir;
-                        }
-                }
-            __syncthreads();
-            return;
-        }
-    {
-        // this iteration's propagate tile size from all running queries' samples
-        uint32_t mine = 0;
-        for(int q = threadIdx.x; q < n; q += blockDim.x)
-            {
-                mine += samples_of(q);
-                if(mine >= pair_samples) mine = pair_samples;
-            }
-        uint32_t total;
-        block_exclusive_scan<kAppendThreads>(mine, scratch, &total);
-        if(threadIdx.x == 0) s_tile_size = total >= pair_samples ? kPropPer * block : block;
-    }
-    if(threadIdx.x == 0) carry[0] = carry[1] = carry[2] = 0;
-    __syncthreads();
-    const uint32_t prop_tile = s_tile_size;
-    for(int base = 0; base < n; base += blockDim.x)
-        {
-            int q = base + threadIdx.x;
-            uint32_t ta = 0, tc = 0, told = 0, run = 0;
-            // other blocks finalised these states in this kernel: read past L1
-            if(q < n && __ldcg(&S[q].status) == KGMT_QUERY_RUNNING)
-                {
-                    uint32_t ns = __ldcg(&S[q].n_samples);
-                    ta = (ns + prop_tile - 1) / prop_tile;
-                    told = (__ldcg(&S[q].tree_size) + kTileOld - 1) / kTileOld;
-                    tc = told + (ns + kTileC - 1) / kTileC;
-                    run = 1;
-                }
-            uint32_t tot_a, tot_c, tot_r;
-            uint32_t ea = block_exclusive_scan<kAppendThreads>(ta, scratch, &tot_a);
-            uint32_t ec = block_exclusive_scan<kAppendThreads>(tc, scratch, &tot_c);
-            block_exclusive_scan<kAppendThreads>(run, scratch, &tot_r);
-            if(q < n)
-                {
-                    tile_a_base[q] = carry[0] + ea;
-                    tile_c_base[q] = carry[1] + ec;
-                    tile_c_old[q] = told;
-                }
-            __syncthreads();
-            if(threadIdx.x == 0)
-                {
-                    carry[0] += tot_a;
-                    carry[1] += tot_c;
-                    carry[2] += tot_r;
-                }
-            __syncthreads();
-        }
-    if(threadIdx.x == 0)
-        {
-            tile_a_base[n] = carry[0];
-            tile_c_base[n] = carry[1];
-            sched->tiles_a = carry[0];
-            sched->tiles_c = carry[1];
-            sched->running = carry[2];
-            sched->ticket_a = 0;
-            sched->prop_tile = prop_tile;
-            if(carry[2]) sched->iterations += 1;
-            if(sched->host_running) *(volatile uint32_t*)sched->host_running = carry[2];
-        }
-    __syncthreads();
-}
-
-// frontier entries R, samples per entry and samples of the next iteration
-// (KGMT.cu:183-201 with the capacity rule made safe)
-__device__ __forceinline__ void plan_samples(const QueryParams& P, QueryState& st)
-{
-    uint32_t R = st.n_react + st.w_new;
-    uint32_t free_slots = P.capacity - st.tree_size;
-    uint32_t spe = 0, ruse = R;
-    if(R > 0)
-        {
-            spe = free_slots / R;
-            if(spe > P.samples_per_node) spe = P.samples_per_node;
-            if(spe == 0)
-                {
-                    spe = 1;
-                    ruse = free_slots;
-                }
-        }
-    st.spe = spe;
-    st.n_samples = ruse * spe;
 }
 
 // ---------------------------------------------------------------------------
@@ -515,255 +238,6 @@ __global__ void k_schedule(const QueryParams* __restrict__ P, const QueryState* 
     compute_schedule(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
 }
 
-// ---------------------------------------------------------------------------
-// propagate (+ the region scores of each query, computed by the block that
-// finishes the query's last propagate tile)
-// ---------------------------------------------------------------------------
-struct PropCtx {
-    uint32_t itr, spe, n_react, n_samples;
-};
-
-constexpr int kSortBins = 32;  // step-count bins of the in-tile sort (last bin: dead lanes)
-
-struct PropShared {
-    uint32_t acc;                // accepted samples of the tile
-    uint32_t steps;              // RK4 steps of the tile
-    uint32_t tests;              // box tests of the tile
-};
-
-// sample rows of a model
-// SAMPLE_DIM and the number of control draws (the step draw follows them,
-// then the accept draw)
-template <int MODEL>
-struct ModelDims {
-    static constexpr int D = MODEL == KGMT_MODEL_QUADROTOR ? 17 : MODEL == KGMT_MODEL_UNICYCLE ? 7 : 10;
-    static constexpr int NC = MODEL == KGMT_MODEL_QUADROTOR ? 4 : 3;
-};
-
-// model bits of the MODELS mask a propagate variant is compiled for
-constexpr int kBitDI = 1, kBitQuad = 2, kBitDubins = 4, kBitUnicycle = 8, kAllModels = 15;
-
-// calls f(std::integral_constant<int, model>) for the query's model, among
-// the models the variant was compiled for (a single-model variant needs no test)
-template <int MODELS, typename F>
-__device__ __forceinline__ void with_model(int model, F&& f)
-{
-    if constexpr((MODELS & kBitDI) != 0)
-        if(MODELS == kBitDI || model == KGMT_MODEL_DOUBLE_INTEGRATOR) f(std::integral_constant<int, KGMT_MODEL_DOUBLE_INTEGRATOR>{});
-    if constexpr((MODELS & kBitQuad) != 0)
-        if(MODELS == kBitQuad || model == KGMT_MODEL_QUADROTOR) f(std::integral_constant<int, KGMT_MODEL_QUADROTOR>{});
-    if constexpr((MODELS & kBitDubins) != 0)
-        if(MODELS == kBitDubins || model == KGMT_MODEL_DUBINS_AIRPLANE) f(std::integral_constant<int, KGMT_MODEL_DUBINS_AIRPLANE>{});
-    if constexpr((MODELS & kBitUnicycle) != 0)
-        if(MODELS == kBitUnicycle || model == KGMT_MODEL_UNICYCLE) f(std::integral_constant<int, KGMT_MODEL_UNICYCLE>{});
-}
-
-template <int MODEL>
-__device__ __forceinline__ bool propagate_model(const QueryParams& p, const GridView& grid, const float* x0, const float* u, const float4* obs,
-                                                uint32_t n_obs, float* x1, PropCount& cnt)
-{
-    if constexpr(MODEL == KGMT_MODEL_QUADROTOR) return propagate_quad(p, grid, x0, u, obs, n_obs, x1, cnt);
-    else if constexpr(MODEL == KGMT_MODEL_DUBINS_AIRPLANE) return propagate_dubins(p, grid, x0, u, obs, n_obs, x1, cnt);
-    else if constexpr(MODEL == KGMT_MODEL_UNICYCLE) return propagate_unicycle(p, grid, x0, u, obs, n_obs, x1, cnt);
-    else return propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
-}
-
-// RK4 steps sample s will take (its step uniform alone), for ordering the
-// samples of a tile so that a warp's lanes loop about equally long
-template <int MODEL>
-__device__ __forceinline__ int sample_steps(const QueryParams& p, const PropCtx& c, uint32_t s)
-{
-    const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-    if constexpr(ModelDims<MODEL>::NC == 4)
-        {
-            const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
-            return draw_steps(p, u01(b.x));
-        }
-    else
-        {
-            const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
-            return draw_steps(p, u01(a.w));
-        }
-}
-
-// gather the parent row and draw the sample's uniforms (no obstacle access,
-// so it runs while the tile's boxes are still in flight)
-template <int MODEL>
-__device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const PropCtx& c, uint32_t s, float* x0, float* u)
-{
-    constexpr int D = ModelDims<MODEL>::D;
-    const uint32_t e = s / c.spe;
-    const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
-    const float* src = p.tree + (size_t)par * D;
-#pragma unroll
-    for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
-    const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-    const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
-    const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
-    u[0] = u01(a.x), u[1] = u01(a.y), u[2] = u01(a.z), u[3] = u01(a.w);
-    u[4] = u01(b.x), u[5] = u01(b.y), u[6] = u01(b.z), u[7] = u01(b.w);
-    return par;
-}
-
-template <int MODEL>
-__device__ __forceinline__ void finish_sample(const QueryParams& p, const GridView& grid, const float4* obs, uint32_t n_obs, uint32_t s,
-                                              bool live, uint32_t par, const float* x0, const float* u, PropShared* sh)
-{
-    constexpr int D = ModelDims<MODEL>::D;
-    constexpr int NC = ModelDims<MODEL>::NC;
-    const unsigned full = 0xffffffffu;
-    int r1 = -1;
-    uint64_t bit = 0ull;
-    PropCount cnt;
-    bool ok = false, acc = false;
-    if(live)
-        {
-            float x1[D];
-            ok = propagate_model<MODEL>(p, grid, x0, u, obs, n_obs, x1, cnt);
-            const CellIds cid = cell_ids(p, x1);
-            r1 = cid.r1;
-            bit = 1ull << cid.r2;
-            // the region's marks and score are loaded before the row stores
-            // (which the compiler must otherwise keep ahead of them)
-            uint64_t marks = 0ull;
-            float score = 0.0f;
-            if(ok)
-                {
-                    marks = p.marks[r1];
-                    score = p.score[r1];
-                }
-            float* dst = p.us + (size_t)s * D;
-#pragma unroll
-            for(int j = 0; j < D; ++j) dst[j] = x1[j];
-            p.up[s] = (int32_t)par;
-            p.ur1[s] = r1;
-            if(ok)
-                {
-                    const bool fresh = (marks & bit) == 0ull;
-                    acc = (u[NC + 1] < score) || fresh;
-                }
-            p.uflag[s] = acc ? 1 : 0;
-        }
-    // warp-aggregated histogram updates: counter over all samples, valid over
-    // the valid ones (KGMT.cu:250-253); tile totals in shared memory
-    const unsigned live_mask = __ballot_sync(full, live);
-    if(live)
-        {
-            const unsigned peers = __match_any_sync(live_mask, r1);
-            if((threadIdx.x & 31) == (__ffs(peers) - 1)) atomicAdd(&p.counter[r1], __popc(peers));
-        }
-    const unsigned ok_mask = __ballot_sync(full, ok);
-    if(ok)
-        {
-            // valid count and the OR of the fine-cell bits, one atomic each per region and warp
-            const unsigned peers = __match_any_sync(ok_mask, r1);
-            const unsigned lo = __reduce_or_sync(peers, (unsigned)bit);
-            const unsigned hi = __reduce_or_sync(peers, (unsigned)(bit >> 32));
-            if((threadIdx.x & 31) == (__ffs(peers) - 1))
-                {
-                    atomicAdd(&p.valid[r1], __popc(peers));
-                    atomicOr((unsigned long long*)&p.newmarks[r1], ((unsigned long long)hi << 32) | lo);
-                }
-        }
-    const unsigned acc_mask = __ballot_sync(full, acc);
-    const unsigned warp_steps = __reduce_add_sync(full, (unsigned)cnt.steps);
-    const unsigned warp_tests = __reduce_add_sync(full, cnt.tests);
-    if((threadIdx.x & 31) == 0)
-        {
-            if(acc_mask) atomicAdd(&sh->acc, (unsigned)__popc(acc_mask));
-            if(warp_steps) atomicAdd(&sh->steps, warp_steps);
-            if(warp_tests) atomicAdd(&sh->tests, warp_tests);
-        }
-}
-
-// Graph::updateVertices (Graph.cu:311-358) for one query, by one block: all
-// regions scored, lane l of kScoreLanes sums regions l, l+256, ... in order,
-// then a halving tree over the lanes.  Histograms and marks were updated by
-// other blocks' atomics in this kernel: read past L1.
-template <int NT>
-__device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes)
-{
-    const float F = (float)p.fine_cells;
-    constexpr int U = 4;  // regions whose loads are issued together
-    // the thread's first U regions keep their raw score in registers for the
-    // normalisation pass (no re-read of what it just wrote)
-    float kept[U];
-    for(int l = threadIdx.x; l < kScoreLanes; l += NT)
-        {
-            float acc = 0.0f;
-            for(uint32_t r0 = (uint32_t)l; r0 < p.regions; r0 += U * kScoreLanes)
-                {
-                    const bool first = l == (int)threadIdx.x && r0 == (uint32_t)l;
-                    uint64_t m[U];
-                    int32_t nv[U], n[U];
-#pragma unroll
-                    for(int k = 0; k < U; ++k)
-                        {
-                            const uint32_t r = r0 + k * kScoreLanes;
-                            if(r < p.regions)
-                                {
-                                    m[k] = __ldcg(&p.marks[r]) | __ldcg(&p.newmarks[r]);
-                                    nv[k] = __ldcg(&p.valid[r]);
-                                    n[k] = __ldcg(&p.counter[r]);
-                                }
-                        }
-                    // regions in increasing order: the lane's sum keeps its fixed order
-#pragma unroll
-                    for(int k = 0; k < U; ++k)
-                        {
-                            const uint32_t r = r0 + k * kScoreLanes;
-                            if(r >= p.regions) break;
-                            p.marks[r] = m[k];
-                            p.newmarks[r] = 0ull;
-                            float raw = 0.0f;    // adds nothing to the total
-                            float keep = -1.0f;  // marks "no valid sample" for the normalisation pass
-                            if(nv[k] > 0)
-                                {
-                                    const float cov = (float)__popcll(m[k]) / F;
-                                    const float a = p.epsilon + (float)nv[k];
-                                    const float b = a + (float)(n[k] - nv[k]);
-                                    const float fv = (a / b) * p.cell_volume;
-                                    const float f2 = fv * fv;
-                                    const float f4 = f2 * f2;
-                                    const float nf = (float)n[k];
-                                    const float den = (1.0f + cov) * (1.0f + nf * nf);
-                                    raw = f4 / den;
-                                    keep = raw;
-                                }
-                            p.score[r] = keep;
-                            if(first) kept[k] = keep;
-                            acc = acc + raw;
-                        }
-                }
-            lanes[l] = acc;
-        }
-    __syncthreads();
-    for(int stride = kScoreLanes / 2; stride >= 1; stride >>= 1)
-        {
-            for(int l = threadIdx.x; l < stride; l += NT) lanes[l] = lanes[l] + lanes[l + stride];
-            __syncthreads();
-        }
-    const float total = lanes[0];
-    // raw score (-1 for regions without valid samples) -> normalised score;
-    // past the registers each lane re-reads only what it wrote itself
-    auto norm = [&](float raw) { return raw < 0.0f ? 1.0f : (total > 0.0f ? p.epsilon + raw / total : p.epsilon); };
-    for(int l = threadIdx.x; l < kScoreLanes; l += NT)
-        {
-            uint32_t r = (uint32_t)l;
-            if(l == (int)threadIdx.x)
-                {
-#pragma unroll
-                    for(int k = 0; k < U; ++k, r += kScoreLanes)
-                        if(r < p.regions) p.score[r] = norm(kept[k]);
-                }
-            for(; r < p.regions; r += kScoreLanes) p.score[r] = norm(p.score[r]);
-        }
-    if(threadIdx.x == 0) st.score_total = total;
-}
-
-// MODELS: bit 0 double integrator present, bit 1 quadrotor present; the
-// launch picks the variant for the admitted mix, so a single-model batch
-// pays for one model's registers only
 template <int NT, int MODELS>
 __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                   const uint32_t* __restrict__ tile_base)
@@ -792,8 +266,8 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
         }
     const uint32_t total = sched->tiles_a;
     const int n_slots = (int)sched->n_slots;
-    // samples per thread this iteration (the schedule sized the tiles)
-    const int per = sched->prop_tile > (uint32_t)NT ? kPropPer : 1;
+    // samples per tile this iteration (the schedule sized the tiles)
+    const uint32_t tile = sched->prop_tile;
     if(blockIdx.x >= total) return;
     if(threadIdx.x == 0)
         {
@@ -859,77 +333,17 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                     cur_q = q;
                 }
             const uint32_t lt = t - bases.base[q];
-            const int model = s_p.model;
-            // counting sort of the tile's kPropPer * NT samples by step count
-            // (dead lanes last); pass 0 gives thread i the i-th shortest, pass
-            // 1 the i-th longest, so every thread gets about the same work
-            // and a warp's lanes loop about equally long in each pass
-            {
-                uint32_t s0[kPropPer], rank[kPropPer];
-                int key[kPropPer];
-                if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = 0;
-#pragma unroll
-                for(int h = 0; h < kPropPer; ++h)
-                    {
-                        // with one sample per thread the second key is a dead lane
-                        s0[h] = h < per ? (lt * per + h) * NT + threadIdx.x : 0xFFFFFFFFu;
-                        key[h] = kSortBins - 1;
-                        if(s0[h] < s_c.n_samples)
-                            {
-                                int k = 1;
-                                with_model<MODELS>(model, [&](auto m) { k = sample_steps<decltype(m)::value>(s_p, s_c, s0[h]); });
-                                key[h] = k < kSortBins - 1 ? k : kSortBins - 2;
-                            }
-                    }
-                __syncthreads();
-#pragma unroll
-                for(int h = 0; h < kPropPer; ++h) rank[h] = atomicAdd(&s_hist[key[h]], 1u);
-                __syncthreads();
-                if(threadIdx.x < 32)
-                    {
-                        // exclusive scan of the bins (kSortBins <= 32)
-                        const uint32_t v = threadIdx.x < kSortBins ? s_hist[threadIdx.x] : 0u;
-                        uint32_t x = v;
-#pragma unroll
-                        for(int o = 1; o < 32; o <<= 1)
-                            {
-                                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                                if(threadIdx.x >= (unsigned)o) x += y;
-                            }
-                        if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = x - v;
-                    }
-                __syncthreads();
-#pragma unroll
-                for(int h = 0; h < kPropPer; ++h) s_perm[s_hist[key[h]] + rank[h]] = s0[h];
-                __syncthreads();
-            }
-            const float4* obs = s_p.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : s_p.obstacles;
-            static_assert(kPropPer == 2, "the passes pair the i-th shortest with the i-th longest sample");
-            for(int pass = 0; pass < per; ++pass)
-                {
-                    // pass 0: the i-th shortest; pass 1: the i-th longest
-                    const uint32_t s = s_perm[pass == 0 ? threadIdx.x : (uint32_t)(2 * NT - 1) - threadIdx.x];
-                    const bool live = s < s_c.n_samples;
-                    float x0[KGMT_MAX_SAMPLE_DIM], u[8];
-                    uint32_t par = 0;
-                    if(live)
+            propagate_tile<NT, MODELS>(s_p, s_c, lt, tile, &s_sh, s_hist, s_perm, s_obs, s_gstart, s_gitems, s_gmeta, [&] {
+                if(!wait_obs) return;
+                uint32_t spins = 0;
+                while(!mbar_try_wait(&bar, phase))
+                    if(++spins > kSpinLimit)
                         {
-                            with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(s_p, s_c, s, x0, u); });
+                            if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
+                            break;
                         }
-                    if(pass == 0 && wait_obs)
-                        {
-                            uint32_t spins = 0;
-                            while(!mbar_try_wait(&bar, phase))
-                                if(++spins > kSpinLimit)
-                                    {
-                                        if(threadIdx.x == 0) atomicOr(&sched->error, kErrCopyTimeout);
-                                        break;
-                                    }
-                            phase ^= 1u;
-                        }
-                    const GridView grid{(s_p.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, s_p.grid_items};
-                    with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(s_p, grid, obs, s_p.n_obstacles, s, live, par, x0, u, &s_sh); });
-                }
+                phase ^= 1u;
+            });
             __syncthreads();
             if(threadIdx.x == 0)
                 {
@@ -954,81 +368,6 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
         }
 }
 
-// ---------------------------------------------------------------------------
-// append / re-activation / frontier build
-// ---------------------------------------------------------------------------
-__device__ void finalize_query(const QueryParams& p, QueryState& st, Sched* sched)
-{
-    // runs on one thread; the per-iteration totals were accumulated by other
-    // blocks' atomics, so they are read past L1
-    const uint32_t acc_total = __ldcg(&st.acc_total);
-    const int32_t goal_cand = __ldcg(&st.goal_cand);
-    if(acc_total != __ldcg(&st.n_next)) atomicOr(&sched->error, kErrAppendMismatch);
-    st.tree_size += acc_total;
-    st.samples_drawn += st.n_samples;
-    if(goal_cand != INT_MAX)
-        {
-            st.status = KGMT_QUERY_SUCCESS;
-            st.goal_index = goal_cand;
-        }
-    else if(st.itr >= p.max_iterations) st.status = KGMT_QUERY_ITER_LIMIT;
-    else if(st.tree_size >= p.capacity) st.status = KGMT_QUERY_CAPACITY;
-    const uint32_t react_total = __ldcg(&st.react_total), w_total = __ldcg(&st.w_total);
-    // per-iteration accumulators start from zero next iteration
-    st.tiles_done = 0;
-    st.prop_done = 0;
-    st.react_total = 0;
-    st.acc_total = 0;
-    st.w_total = 0;
-    st.goal_cand = INT_MAX;
-    if(st.status != KGMT_QUERY_RUNNING)
-        {
-            st.t_end = globaltimer();
-            return;
-        }
-    st.n_react = react_total;
-    st.w_new = w_total;
-    st.itr += 1;
-    st.n_next = 0;
-    plan_samples(p, st);
-}
-
-// Copies one sample row (written by the propagate kernel, read-only here)
-// into the tree and returns its goal distance.  The row is read into
-// registers before the first store: the two buffers might alias as far as
-// the compiler can tell, so interleaved loads would each wait for the
-// previous store's turn.
-template <int D>
-__device__ __forceinline__ float append_row_d(const QueryParams& p, const float* src, float* dst)
-{
-    float r[D];
-#pragma unroll
-    for(int c = 0; c < D; ++c) r[c] = __ldg(src + c);
-#pragma unroll
-    for(int c = 0; c < D; ++c) dst[c] = r[c];
-    return goal_distance(p, r);
-}
-
-__device__ __forceinline__ float append_row(const QueryParams& p, const float* src, float* dst, int D)
-{
-    switch(D)
-        {
-            case 7: return append_row_d<7>(p, src, dst);
-            case 17: return append_row_d<17>(p, src, dst);
-            default: return append_row_d<10>(p, src, dst);
-        }
-}
-
-// KGMT.cu:387-388
-__device__ __forceinline__ float f_accept_of(const QueryParams& p, const QueryState& st)
-{
-    const float ta = 1.0f - (float)(st.tree_size + st.n_next) / (float)p.capacity;
-    const float ie = (float)st.itr * p.epsilon;
-    const double t = (double)ta;
-    const double t5 = ((t * t) * (t * t)) * t;
-    return (float)((double)ie * t5);
-}
-
 __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                            uint32_t* tile_a_base, uint32_t* tile_c_base, uint32_t* tile_c_old)
 {
@@ -1040,6 +379,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
     __shared__ uint32_t s_cold[kBaseCache];
     const uint32_t total = sched->tiles_c;
     const int n_slots = (int)sched->n_slots;
+    const uint32_t old_tile = sched->old_tile;
     if(blockIdx.x >= total) return;
     // this iteration's tile bases (the schedule rewrites the global arrays only
     // after every tile is done)
@@ -1073,7 +413,9 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             if(lt < n_old)
                 {
                     // ---- re-activation of old nodes (KGMT.cu:364-377) ----
-                    const uint32_t i0 = lt * kTileOld + threadIdx.x * kOldPer;
+                    // old_tile / kAppendThreads consecutive nodes a thread (4 or 16)
+                    const uint32_t per_t = old_tile / kAppendThreads;
+                    const uint32_t i0 = lt * old_tile + threadIdx.x * per_t;
                     const float fa = s_fa;
                     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
                     uint32_t flags = 0, cnt = 0;
@@ -1085,7 +427,8 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     for(int g = 0; g < kOldPer; g += 4)
                         {
                             const uint32_t ib = i0 + g;
-                            if(ib + 3 < tree_size)
+                            if((uint32_t)g >= per_t) reg[g] = reg[g + 1] = reg[g + 2] = reg[g + 3] = 0;
+                            else if(ib + 3 < tree_size)
                                 {
                                     const int4 v = *(const int4*)(p.node_r1 + ib);
                                     reg[g] = v.x, reg[g + 1] = v.y, reg[g + 2] = v.z, reg[g + 3] = v.w;
@@ -1100,7 +443,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     for(int j = 0; j < kOldPer; ++j)
                         {
                             const uint32_t i = i0 + j;
-                            if(i < tree_size)
+                            if((uint32_t)j < per_t && i < tree_size)
                                 {
                                     const U4 r = philox4x32_10(i, itr, 1u, 0u, k0, k1);
                                     const float ur = u01(r.x);

@@ -134,6 +134,8 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
     sched.prop_tile = block;
     sched.prop_block = block;
     sched.pair_samples = 2u * (uint32_t)grid_a * block;
+    sched.n_sms = (uint32_t)sms;
+    sched.old_tile = kTileOld;
     NA_CHECK(cuda_status(cudaMemcpyAsync(d_params, &params, sizeof(params), cudaMemcpyHostToDevice, s), "upload(params)"));
     NA_CHECK(cuda_status(cudaMemcpyAsync(d_sched, &sched, sizeof(sched), cudaMemcpyHostToDevice, s), "upload(sched)"));
     NA_CHECK(cuda_status(cudaMemsetAsync(d_state, 0xFF, sizeof(QueryState), s), "memset(state)"));

@@ -19,9 +19,12 @@ constexpr int kTileC = 1024;            // samples per append tile
 constexpr int kAppendThreads = 256;     // threads per append block
 constexpr int kAppendPer = kTileC / kAppendThreads;  // samples per append thread
 // old nodes per re-activation tile: larger than an append tile, so the fixed
-// latency of a tile (loads, scan, look-back, hand-over) covers more nodes
+// latency of a tile (loads, scan, look-back, hand-over) covers more nodes;
+// small tiles (4 nodes a thread) while all running queries' old nodes fill
+// fewer large tiles than there are SMs, so few trees still spread out
 constexpr int kTileOld = 4096;
-constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread
+constexpr int kTileOldSmall = 1024;
+constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread, at most
 // samples per propagate thread and tile in iterations with enough samples to
 // fill the resident threads twice: a tile of kPropPer * NT samples is sorted
 // by step count and thread t runs the t-th shortest and the t-th longest, so
@@ -170,9 +173,11 @@ struct Sched {
     uint32_t finalized;
     uint32_t error;
     uint32_t iterations;  // engine iterations launched with work
-    uint32_t prop_tile;   // samples per propagate tile this iteration: prop_block, or kPropPer x prop_block
+    uint32_t prop_tile;   // samples per propagate tile this iteration: 32..prop_block (a power of two), or kPropPer x prop_block
     uint32_t prop_block;  // propagate block size
     uint32_t pair_samples;  // iterations with at least this many samples use kPropPer samples per thread
+    uint32_t n_sms;         // SMs of the device: smaller iterations use smaller tiles, about one per SM
+    uint32_t old_tile;      // old nodes per re-activation tile this iteration: kTileOld or kTileOldSmall
     // mapped pinned host word that mirrors `running` (or null): the host polls
     // it without a copy in the stream between graph replays
     uint32_t* host_running;
