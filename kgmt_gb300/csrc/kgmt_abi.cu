@@ -212,6 +212,7 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
                          "stage obstacles"));
     p->eng.host_params(0) = p->params;
     p->eng.set_models(Engine::model_bit(p->cfg.model));
+    p->eng.set_max_obstacles(n_obstacles);
     CHECK_ST(p->eng.admit(0, 1, 1));
     CHECK_ST(p->eng.run_until_done(p->cfg.max_iterations));
     CHECK_ST(p->eng.extract_paths(1));
@@ -322,7 +323,7 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
     RETURN_IF(!cfgs || !obs_offset || !obs_count, KGMT_ERR_INVALID_ARG, "batch: NULL argument");
     b->eng.reset_counters();
     uint64_t boxes = 0;
-    uint32_t max_iters = 0;
+    uint32_t max_iters = 0, max_obs = 0;
     size_t total = 0;
     std::vector<QueryLayout> L(n);
     for(uint32_t i = 0; i < n; ++i)
@@ -332,6 +333,7 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
             total += L[i].total;
             uint64_t end = (uint64_t)obs_offset[i] + obs_count[i];
             if(end > boxes) boxes = end;
+            if(obs_count[i] > max_obs) max_obs = obs_count[i];
             if(cfgs[i].max_iterations > max_iters) max_iters = cfgs[i].max_iterations;
         }
     RETURN_IF(boxes > (1ull << 31), KGMT_ERR_INVALID_ARG, "batch: too many obstacles");
@@ -346,6 +348,7 @@ static kgmt_status batch_prepare(kgmt_batch* b, uint32_t n, const kgmt_config* c
     int models = 0;
     for(uint32_t i = 0; i < n; ++i) models |= Engine::model_bit(cfgs[i].model);
     b->eng.set_models(models);
+    b->eng.set_max_obstacles(max_obs);
     b->params.resize(n);
     for(uint32_t i = 0; i < n; ++i)
         {

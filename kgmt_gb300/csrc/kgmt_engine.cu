@@ -427,6 +427,18 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     return KGMT_OK;
 }
 
+void Engine::set_max_obstacles(uint32_t max_obs)
+{
+    const uint32_t boxes = smem_boxes_for(max_obs);
+    if(boxes == smem_boxes_) return;
+    smem_boxes_ = boxes;
+    if(graph_)
+        {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+}
+
 void Engine::set_models(int mask)
 {
     mask = variant_of(mask & 15);
@@ -528,7 +540,7 @@ kgmt_status Engine::launch_iteration()
                     if(st != KGMT_OK) return st;
                     prof_kind_.push_back(k);
                 }
-            if(k == 0) KGMT_CUDA(launch_propagate(a, (int)prop_block_, models_, grid_a_[models_], stream_), "k_propagate");
+            if(k == 0) KGMT_CUDA(launch_propagate(a, (int)prop_block_, models_, grid_a_[models_], smem_boxes_, stream_), "k_propagate");
             else KGMT_CUDA(launch_append(a, grid_c_, stream_), "k_append");
             if(profile_)
                 {

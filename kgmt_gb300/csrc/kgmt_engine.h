@@ -97,6 +97,9 @@ class Engine {
     // kernel variant (single-model variants, or the one for any mix); a
     // change drops the graph
     void set_models(int mask);
+    // largest box count of the admitted queries: sizes the propagate kernel's
+    // shared-memory box stage (a change drops the graph)
+    void set_max_obstacles(uint32_t max_obs);
     static int model_bit(int32_t model)
     {
         return model == KGMT_MODEL_QUADROTOR ? 2 : model == KGMT_MODEL_DUBINS_AIRPLANE ? 4 : model == KGMT_MODEL_UNICYCLE ? 8 : 1;
@@ -128,6 +131,7 @@ class Engine {
     int grid_a_[16] = {};           // propagate grid per variant
     int grid_c_ = 0;
     int models_ = 15;               // propagate variant (Engine::variant_of)
+    uint32_t smem_boxes_ = kSmemObstacles;  // boxes staged in shared memory per propagate block
     QueryParams* d_params_ = nullptr;
     QueryState* d_states_ = nullptr;
     Sched* d_sched_ = nullptr;

@@ -391,28 +391,30 @@ __device__ __forceinline__ bool propagate_model(const QueryParams& p, const Grid
     else return propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
 }
 
-// RK4 steps sample s will take (its step uniform alone), for ordering the
-// samples of a tile so that a warp's lanes loop about equally long
+// A sample's eight uniforms come from two Philox blocks, (s, itr, 0, 0) and
+// (s, itr, 0, 1): controls first, then the step draw, then the accept draw.
+// The block holding the step draw ("key block": the first for three
+// controls, the second for four) is drawn once, when the tile is sorted by
+// step count, and handed to the thread that propagates the sample.
 template <int MODEL>
-__device__ __forceinline__ int sample_steps(const QueryParams& p, const PropCtx& c, uint32_t s)
+__device__ __forceinline__ U4 sample_key_block(const QueryParams& p, const PropCtx& c, uint32_t s)
 {
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-    if constexpr(ModelDims<MODEL>::NC == 4)
-        {
-            const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
-            return draw_steps(p, u01(b.x));
-        }
-    else
-        {
-            const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
-            return draw_steps(p, u01(a.w));
-        }
+    return philox4x32_10(s, c.itr, 0u, ModelDims<MODEL>::NC == 4 ? 1u : 0u, k0, k1);
+}
+
+// RK4 steps of the sample whose key block is kb, for ordering the samples of
+// a tile so that a warp's lanes loop about equally long
+template <int MODEL>
+__device__ __forceinline__ int sample_steps(const QueryParams& p, const U4& kb)
+{
+    return draw_steps(p, u01(ModelDims<MODEL>::NC == 4 ? kb.x : kb.w));
 }
 
 // gather the parent row and draw the sample's uniforms (no obstacle access,
-// so it runs while the tile's boxes are still in flight)
+// so it runs while the tile's boxes are still in flight); kb: its key block
 template <int MODEL>
-__device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const PropCtx& c, uint32_t s, float* x0, float* u)
+__device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const PropCtx& c, uint32_t s, const U4& kb, float* x0, float* u)
 {
     constexpr int D = ModelDims<MODEL>::D;
     const uint32_t e = s / c.spe;
@@ -421,8 +423,10 @@ __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const P
 #pragma unroll
     for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
-    const U4 a = philox4x32_10(s, c.itr, 0u, 0u, k0, k1);
-    const U4 b = philox4x32_10(s, c.itr, 0u, 1u, k0, k1);
+    constexpr bool four = ModelDims<MODEL>::NC == 4;
+    const U4 other = philox4x32_10(s, c.itr, 0u, four ? 0u : 1u, k0, k1);
+    const U4& a = four ? other : kb;
+    const U4& b = four ? kb : other;
     u[0] = u01(a.x), u[1] = u01(a.y), u[2] = u01(a.z), u[3] = u01(a.w);
     u[4] = u01(b.x), u[5] = u01(b.y), u[6] = u01(b.z), u[7] = u01(b.w);
     return par;
@@ -509,8 +513,8 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
 // and draws (the boxes' bulk copy may be in flight until then).
 // Block-uniform call.
 template <int NT, int MODELS, typename Wait>
-__device__ __forceinline__ void propagate_tile(const QueryParams& sp, const PropCtx& sc, uint32_t lt, uint32_t tile, PropShared* sh,
-                                               uint32_t* s_hist, uint32_t* s_perm, const float4* s_obs, const uint16_t* s_gstart,
+__device__ __forceinline__ void propagate_tile(const QueryParams& sp, const PropCtx& sc, uint32_t lt, uint32_t tile, uint32_t smem_boxes, PropShared* sh,
+                                               uint32_t* s_hist, uint32_t* s_perm, uint4* s_key, const float4* s_obs, const uint16_t* s_gstart,
                                                const uint16_t* s_gitems, const uint32_t* s_gmeta, Wait&& wait)
 {
     const int model = sp.model;
@@ -518,6 +522,7 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
     {
         uint32_t s0[kPropPer], rank[kPropPer];
         int key[kPropPer];
+        U4 kb[kPropPer];
         if(threadIdx.x < kSortBins) s_hist[threadIdx.x] = 0;
 #pragma unroll
         for(int h = 0; h < kPropPer; ++h)
@@ -526,10 +531,14 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
                 if(per == kPropPer) s0[h] = (lt * kPropPer + h) * NT + threadIdx.x;
                 else s0[h] = (h == 0 && threadIdx.x < tile) ? lt * tile + threadIdx.x : 0xFFFFFFFFu;
                 key[h] = kSortBins - 1;
+                kb[h] = U4{0u, 0u, 0u, 0u};
                 if(s0[h] < sc.n_samples)
                     {
                         int k = 1;
-                        with_model<MODELS>(model, [&](auto m) { k = sample_steps<decltype(m)::value>(sp, sc, s0[h]); });
+                        with_model<MODELS>(model, [&](auto m) {
+                            kb[h] = sample_key_block<decltype(m)::value>(sp, sc, s0[h]);
+                            k = sample_steps<decltype(m)::value>(sp, kb[h]);
+                        });
                         key[h] = k < kSortBins - 1 ? k : kSortBins - 2;
                     }
             }
@@ -552,18 +561,29 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
             }
         __syncthreads();
 #pragma unroll
-        for(int h = 0; h < kPropPer; ++h) s_perm[s_hist[key[h]] + rank[h]] = s0[h];
+        for(int h = 0; h < kPropPer; ++h)
+            {
+                const uint32_t pos = s_hist[key[h]] + rank[h];
+                s_perm[pos] = s0[h];
+                s_key[pos] = make_uint4(kb[h].x, kb[h].y, kb[h].z, kb[h].w);
+            }
         __syncthreads();
     }
-    const float4* obs = sp.n_obstacles <= (uint32_t)kSmemObstacles ? s_obs : sp.obstacles;
+    const float4* obs = sp.n_obstacles <= smem_boxes ? s_obs : sp.obstacles;
     static_assert(kPropPer == 2, "the passes pair the i-th shortest with the i-th longest sample");
     for(int pass = 0; pass < per; ++pass)
         {
-            const uint32_t s = s_perm[pass == 0 ? threadIdx.x : (uint32_t)(2 * NT - 1) - threadIdx.x];
+            const uint32_t slot = pass == 0 ? threadIdx.x : (uint32_t)(2 * NT - 1) - threadIdx.x;
+            const uint32_t s = s_perm[slot];
             const bool live = s < sc.n_samples;
             float x0[KGMT_MAX_SAMPLE_DIM], u[8];
             uint32_t par = 0;
-            if(live) with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(sp, sc, s, x0, u); });
+            if(live)
+                {
+                    const uint4 k4 = s_key[slot];
+                    const U4 kb1{k4.x, k4.y, k4.z, k4.w};
+                    with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(sp, sc, s, kb1, x0, u); });
+                }
             if(pass == 0) wait();
             const GridView grid{(sp.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, sp.grid_items};
             with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(sp, grid, obs, sp.n_obstacles, s, live, par, x0, u, sh); });

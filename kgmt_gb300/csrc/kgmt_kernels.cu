@@ -240,14 +240,15 @@ __global__ void k_schedule(const QueryParams* __restrict__ P, const QueryState* 
 
 template <int NT, int MODELS>
 __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_propagate(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
-                                                  const uint32_t* __restrict__ tile_base)
+                                                  const uint32_t* __restrict__ tile_base, uint32_t smem_boxes)
 {
-    // dynamic shared memory: boxes | grid starts | grid items | grid meta
+    // dynamic shared memory: grid starts | grid items | grid meta | boxes
+    // (smem_boxes of them; a query with more reads its boxes from global memory)
     extern __shared__ float4 s_dyn[];
-    float4* s_obs = s_dyn;
-    uint16_t* s_gstart = (uint16_t*)((char*)s_dyn + kSmemObsBytes);
-    uint16_t* s_gitems = (uint16_t*)((char*)s_dyn + kSmemObsBytes + kSmemStartBytes);
-    uint32_t* s_gmeta = (uint32_t*)((char*)s_dyn + kSmemObsBytes + kSmemStartBytes + kSmemItemBytes);
+    uint16_t* s_gstart = (uint16_t*)s_dyn;
+    uint16_t* s_gitems = (uint16_t*)((char*)s_dyn + kSmemStartBytes);
+    uint32_t* s_gmeta = (uint32_t*)((char*)s_dyn + kSmemStartBytes + kSmemItemBytes);
+    float4* s_obs = (float4*)((char*)s_dyn + kSmemGridBytes);
     __shared__ uint32_t s_copy;
     __shared__ alignas(8) uint64_t bar;
     __shared__ QueryParams s_p;
@@ -257,6 +258,7 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
     __shared__ uint32_t s_base[kBaseCache];
     __shared__ uint32_t s_hist[kSortBins];
     __shared__ uint32_t s_perm[kPropPer * NT];
+    __shared__ uint4 s_key[kPropPer * NT];  // key Philox block of each sorted sample
     __shared__ int s_tile, s_q, s_last;
     if(blockIdx.x == 0 && threadIdx.x == 0)
         {
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                             // items: one mbarrier transaction of bulk copies
                             const QueryParams& gp = P[q];
                             const uint32_t n_obs = gp.n_obstacles;
-                            const bool obs_s = n_obs > 0 && n_obs <= (uint32_t)kSmemObstacles;
+                            const bool obs_s = n_obs > 0 && n_obs <= smem_boxes;
                             const bool grid = gp.grid_meta != nullptr;
                             const uint32_t bytes = (obs_s ? n_obs * 32u : 0u) + (grid ? 16u + kSmemStartBytes + kSmemItemBytes : 0u);
                             s_copy = bytes;
@@ -333,7 +335,7 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                     cur_q = q;
                 }
             const uint32_t lt = t - bases.base[q];
-            propagate_tile<NT, MODELS>(s_p, s_c, lt, tile, &s_sh, s_hist, s_perm, s_obs, s_gstart, s_gitems, s_gmeta, [&] {
+            propagate_tile<NT, MODELS>(s_p, s_c, lt, tile, smem_boxes, &s_sh, s_hist, s_perm, s_key, s_obs, s_gstart, s_gitems, s_gmeta, [&] {
                 if(!wait_obs) return;
                 uint32_t spins = 0;
                 while(!mbar_try_wait(&bar, phase))
@@ -655,49 +657,64 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
 // host-side launch wrappers
 // ---------------------------------------------------------------------------
 template <int NT, int MODELS>
-static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, cudaStream_t s)
+static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, uint32_t boxes, cudaStream_t s)
 {
-    k_propagate<NT, MODELS><<<grid, NT, kPropSmemBytes, s>>>(a.params, a.states, a.sched, a.tile_a_base);
+    k_propagate<NT, MODELS><<<grid, NT, prop_smem_bytes(boxes), s>>>(a.params, a.states, a.sched, a.tile_a_base, boxes);
     return cudaGetLastError();
 }
 
 template <int NT>
-static cudaError_t launch_propagate_m(const LaunchArgs& a, int models, int grid, cudaStream_t s)
+static cudaError_t launch_propagate_m(const LaunchArgs& a, int models, int grid, uint32_t boxes, cudaStream_t s)
 {
     switch(models)
         {
-            case kBitDI: return launch_propagate_t<NT, kBitDI>(a, grid, s);
-            case kBitQuad: return launch_propagate_t<NT, kBitQuad>(a, grid, s);
-            case kBitDubins: return launch_propagate_t<NT, kBitDubins>(a, grid, s);
-            case kBitUnicycle: return launch_propagate_t<NT, kBitUnicycle>(a, grid, s);
-            default: return launch_propagate_t<NT, kAllModels>(a, grid, s);
+            case kBitDI: return launch_propagate_t<NT, kBitDI>(a, grid, boxes, s);
+            case kBitQuad: return launch_propagate_t<NT, kBitQuad>(a, grid, boxes, s);
+            case kBitDubins: return launch_propagate_t<NT, kBitDubins>(a, grid, boxes, s);
+            case kBitUnicycle: return launch_propagate_t<NT, kBitUnicycle>(a, grid, boxes, s);
+            default: return launch_propagate_t<NT, kAllModels>(a, grid, boxes, s);
         }
 }
 
-cudaError_t launch_propagate(const LaunchArgs& a, int block, int models, int grid, cudaStream_t s)
+cudaError_t launch_propagate(const LaunchArgs& a, int block, int models, int grid, uint32_t smem_boxes, cudaStream_t s)
 {
+    const uint32_t boxes = smem_boxes < kSmemBoxesMin ? kSmemBoxesMin : smem_boxes > (uint32_t)kSmemObstacles ? (uint32_t)kSmemObstacles : smem_boxes;
     switch(block)
         {
-            case 128: return launch_propagate_m<128>(a, models, grid, s);
-            case 512: return launch_propagate_m<512>(a, models, grid, s);
-            default: return launch_propagate_m<256>(a, models, grid, s);
+            case 128: return launch_propagate_m<128>(a, models, grid, boxes, s);
+            case 512: return launch_propagate_m<512>(a, models, grid, boxes, s);
+            default: return launch_propagate_m<256>(a, models, grid, boxes, s);
         }
+}
+
+// blocks of one variant per SM; also lets the variant take its dynamic
+// shared memory on top of more than 48 KB in total (the launch wrappers run
+// after this has been called for the variant)
+template <int NT, int MODELS>
+static int occupancy_t()
+{
+    int n = 0;
+    const size_t smem = kPropSmemBytes;
+    if(cudaFuncSetAttribute(k_propagate<NT, MODELS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return 0;
+        }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, MODELS>, NT, smem);
+    return n;
 }
 
 template <int NT>
 static int occupancy_m(int models)
 {
-    int n = 0;
-    const size_t smem = kPropSmemBytes;
     switch(models)
         {
-            case kBitDI: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitDI>, NT, smem); break;
-            case kBitQuad: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitQuad>, NT, smem); break;
-            case kBitDubins: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitDubins>, NT, smem); break;
-            case kBitUnicycle: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kBitUnicycle>, NT, smem); break;
-            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_propagate<NT, kAllModels>, NT, smem); break;
+            case kBitDI: return occupancy_t<NT, kBitDI>();
+            case kBitQuad: return occupancy_t<NT, kBitQuad>();
+            case kBitDubins: return occupancy_t<NT, kBitDubins>();
+            case kBitUnicycle: return occupancy_t<NT, kBitUnicycle>();
+            default: return occupancy_t<NT, kAllModels>();
         }
-    return n;
 }
 
 int propagate_blocks_per_sm(int block, int models)

@@ -18,7 +18,9 @@ struct LaunchArgs {
 cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s);
 cudaError_t launch_schedule(const LaunchArgs& a, cudaStream_t s);
 // models: bit 0 double integrator, bit 1 quadrotor (the mix the launch may meet)
-cudaError_t launch_propagate(const LaunchArgs& a, int block, int models, int grid, cudaStream_t s);
+// smem_boxes: boxes a block stages in shared memory (the largest query of the
+// launch, rounded by smem_boxes_for); more are read from global memory
+cudaError_t launch_propagate(const LaunchArgs& a, int block, int models, int grid, uint32_t smem_boxes, cudaStream_t s);
 cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s);
 // src: rows of 2 * ws_dims floats (min corner, max corner)

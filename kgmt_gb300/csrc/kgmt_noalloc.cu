@@ -152,7 +152,7 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
         {
             for(int k = 0; k < 4; ++k)
                 {
-                    NA_CHECK(cuda_status(launch_propagate(a, (int)block, models, grid_a, s), "k_propagate"));
+                    NA_CHECK(cuda_status(launch_propagate(a, (int)block, models, grid_a, smem_boxes_for(n_obstacles), s), "k_propagate"));
                     NA_CHECK(cuda_status(launch_append(a, grid_c, s), "k_append"));
                 }
             NA_CHECK(cuda_status(cudaMemcpyAsync(&running, &d_sched->running, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "poll"));

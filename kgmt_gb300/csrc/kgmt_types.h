@@ -67,11 +67,23 @@ constexpr uint32_t kGridMaxVisit = 8;       // cells a step box may visit before
 constexpr uint32_t kMaxObstacles = 65535;   // grid items are 16-bit box indices
 constexpr uint32_t kMaxGridItems = 65535;   // grid starts are 16-bit
 constexpr uint32_t kSmemGridItems = 4096;   // grid items staged in shared memory per block
-// dynamic shared memory of k_propagate: boxes, grid starts, grid items, meta
-constexpr uint32_t kSmemObsBytes = kSmemObstacles * 32;
+// dynamic shared memory of k_propagate: grid starts, grid items, grid meta,
+// then the boxes -- as many as the launch's box capacity, a power of two
+// from kSmemBoxesMin to kSmemObstacles sized to the admitted queries (what
+// shared memory the boxes leave unused stays L1 cache)
 constexpr uint32_t kSmemStartBytes = ((kGridCells + 1) * 2 + 15) / 16 * 16;
 constexpr uint32_t kSmemItemBytes = kSmemGridItems * 2;
-constexpr uint32_t kPropSmemBytes = kSmemObsBytes + kSmemStartBytes + kSmemItemBytes + 16;
+constexpr uint32_t kSmemGridBytes = kSmemStartBytes + kSmemItemBytes + 16;
+constexpr uint32_t kSmemBoxesMin = 64;
+constexpr uint32_t kPropSmemBytes = kSmemGridBytes + kSmemObstacles * 32;  // the largest launch
+__host__ __device__ constexpr uint32_t prop_smem_bytes(uint32_t boxes) { return kSmemGridBytes + boxes * 32; }
+// box capacity for queries of at most max_obs boxes
+inline uint32_t smem_boxes_for(uint32_t max_obs)
+{
+    uint32_t c = kSmemBoxesMin;
+    while(c < max_obs && c < (uint32_t)kSmemObstacles) c <<= 1;
+    return c;
+}
 
 // error bits in Sched::error
 constexpr uint32_t kErrLookbackTimeout = 1u;
