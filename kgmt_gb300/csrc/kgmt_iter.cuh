@@ -58,6 +58,13 @@ __device__ __forceinline__ unsigned long long globaltimer()
     return t;
 }
 
+// programmatic dependent launch: the kernel that follows in the stream may
+// be scheduled once every block of this one has called pdl_trigger (or
+// exited); pdl_wait blocks until the kernel before this one has completed
+// and its memory is visible (immediately when launched without the attribute)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p)
 {
     return *(const volatile unsigned long long*)p;
@@ -81,7 +88,7 @@ struct BaseCache {
 __device__ __forceinline__ BaseCache cache_bases(const uint32_t* __restrict__ g, int n, uint32_t* s)
 {
     if(n + 1 > kBaseCache) return {g, n};
-    for(int i = threadIdx.x; i <= n; i += blockDim.x) s[i] = g[i];
+    for(int i = threadIdx.x; i <= n; i += blockDim.x) s[i] = __ldcg(g + i);
     __syncthreads();
     return {s, n};
 }

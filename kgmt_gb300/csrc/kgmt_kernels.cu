@@ -260,6 +260,11 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
     __shared__ uint32_t s_perm[kPropPer * NT];
     __shared__ uint4 s_key[kPropPer * NT];  // key Philox block of each sorted sample
     __shared__ int s_tile, s_q, s_last;
+    // everything here depends on the append kernel before this one (its
+    // schedule, frontier and tree); once that is complete the append kernel
+    // after this one may be scheduled into the SMs this launch leaves free
+    pdl_wait();
+    pdl_trigger();
     if(blockIdx.x == 0 && threadIdx.x == 0)
         {
             // counters of the append kernel that follows this one
@@ -387,6 +392,12 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
     // after every tile is done)
     const BaseCache cbase = cache_bases(tile_c_base, n_slots, s_cbase);
     const BaseCache cold = cache_bases(tile_c_old, n_slots - 1, s_cold);
+    // the schedule and tile bases above come from the append kernel before
+    // the propagate kernel this one follows (complete before that propagate
+    // kernel let this one start); the propagate kernel's own results are
+    // read only from here on
+    pdl_wait();
+    pdl_trigger();
     // First tile static, then tickets, taken only when the block is free: a
     // ticket taken ahead would hold a tile that its successors' look-back
     // waits for behind the block's current tile.
@@ -656,11 +667,28 @@ __global__ void k_propagate_samples(const QueryParams p, const float* __restrict
 // ---------------------------------------------------------------------------
 // host-side launch wrappers
 // ---------------------------------------------------------------------------
+// launch as a programmatic dependent of the kernel before it in the stream
+// (the kernel body waits for that one with pdl_wait)
+static cudaLaunchConfig_t dependent_config(int grid, int block, size_t smem, cudaStream_t s, cudaLaunchAttribute* attr)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid, 1, 1);
+    cfg.blockDim = dim3((unsigned)block, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
 template <int NT, int MODELS>
 static cudaError_t launch_propagate_t(const LaunchArgs& a, int grid, uint32_t boxes, cudaStream_t s)
 {
-    k_propagate<NT, MODELS><<<grid, NT, prop_smem_bytes(boxes), s>>>(a.params, a.states, a.sched, a.tile_a_base, boxes);
-    return cudaGetLastError();
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = dependent_config(grid, NT, prop_smem_bytes(boxes), s, attr);
+    return cudaLaunchKernelEx(&cfg, k_propagate<NT, MODELS>, a.params, a.states, a.sched, (const uint32_t*)a.tile_a_base, boxes);
 }
 
 template <int NT>
@@ -738,8 +766,9 @@ int append_blocks_per_sm()
 
 cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s)
 {
-    k_append<<<grid, kAppendThreads, 0, s>>>(a.params, a.states, a.sched, a.tile_a_base, a.tile_c_base, a.tile_c_old);
-    return cudaGetLastError();
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = dependent_config(grid, kAppendThreads, 0, s, attr);
+    return cudaLaunchKernelEx(&cfg, k_append, a.params, a.states, a.sched, a.tile_a_base, a.tile_c_base, a.tile_c_old);
 }
 
 cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s)
