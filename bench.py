@@ -137,10 +137,10 @@ class ClockSampler:
 # DRAM bytes (read + write) per k_propagate launch on this workload, from one
 # ncu capture of a planning step (dram__bytes_read.sum + dram__bytes_write.sum
 # summed over its 132 propagate launches, --cache-control none --clock-control
-# none): 702 MB read + 2085 MB written.  The live algorithmic bytes per launch
+# none): 694 MB read + 2096 MB written.  The live algorithmic bytes per launch
 # (sample rows, parent, region and flag written; parent rows and frontier
 # indices read) are reported beside it.
-PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (702.31e6 + 2084.89e6) / 132
+PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (694.43e6 + 2096.29e6) / 132
 # algorithmic bytes per double-integrator sample: row (10 floats), parent,
 # region and flag written; the parent's row and its frontier index read
 PROPAGATE_BYTES_PER_SAMPLE = 10 * 4 + 4 + 4 + 1 + 10 * 4 + 4
