@@ -186,7 +186,10 @@ __device__ __forceinline__ uint3 block_exclusive_scan3(uint3 v, uint3* scratch, 
 // count, and this iteration's tile sizes.  All threads of the calling block
 // must enter.
 // ---------------------------------------------------------------------------
-template <int NT = kAppendThreads>
+// TOTALS: the finalisers of this iteration accumulated the running queries'
+// samples and tree sizes in Sched::next_samples / next_tree (else a first
+// pass over the slots sums them)
+template <int NT = kAppendThreads, bool TOTALS = false>
 __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryState* __restrict__ S, Sched* sched, uint32_t* tile_a_base,
                                  uint32_t* tile_c_base, uint32_t* tile_c_old)
 {
@@ -234,6 +237,8 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
         sched->ticket_a = 0;
         sched->prop_tile = prop_tile;
         sched->old_tile = old_tile;
+        sched->next_samples = 0ull;
+        sched->next_tree = 0ull;
         if(running) sched->iterations += 1;
         if(sched->host_running) *(volatile uint32_t*)sched->host_running = running;
     };
@@ -252,8 +257,9 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
                     uint32_t ta = 0, tc = 0, told = 0;
                     if(run)
                         {
-                            ta = (ns + prop_tile - 1) / prop_tile;
-                            told = (tree + old_tile - 1) / old_tile;
+                            // tile sizes are powers of two
+                            ta = (ns + prop_tile - 1) >> (__ffs(prop_tile) - 1);
+                            told = (tree + old_tile - 1) >> (__ffs(old_tile) - 1);
                             tc = told + (ns + kTileC - 1) / kTileC;
                         }
                     uint32_t ia = ta, ic = tc, ir = run;
@@ -279,18 +285,29 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
     // pass 1: the running queries' samples and tree sizes, for the tile sizes
     // (a block of slots or fewer keeps its loads in registers for pass 2)
     uint32_t ns0 = 0, tree0 = 0, run0 = 0;
-    uint3 part = make_uint3(0u, 0u, 0u);
-    for(int q = threadIdx.x; q < n; q += NT)
+    uint3 tot = make_uint3(0u, 0u, 0u);
+    if(TOTALS)
         {
-            uint32_t ns, tree;
-            const uint32_t run = load(q, ns, tree);
-            if(q == (int)threadIdx.x) ns0 = ns, tree0 = tree, run0 = run;
-            part.x = min(part.x + min(ns, kClamp), kClamp);
-            part.y = min(part.y + min(tree, kClamp), kClamp);
+            const unsigned long long a = __ldcg(&sched->next_samples), b = __ldcg(&sched->next_tree);
+            tot.x = a < kClamp ? (uint32_t)a : kClamp;
+            tot.y = b < kClamp ? (uint32_t)b : kClamp;
+            if(threadIdx.x < n) run0 = load((int)threadIdx.x, ns0, tree0);
         }
-    uint3 tot;
-    block_exclusive_scan3<NT>(part, s_scan, &tot);
+    else
+        {
+            uint3 part = make_uint3(0u, 0u, 0u);
+            for(int q = threadIdx.x; q < n; q += NT)
+                {
+                    uint32_t ns, tree;
+                    const uint32_t run = load(q, ns, tree);
+                    if(q == (int)threadIdx.x) ns0 = ns, tree0 = tree, run0 = run;
+                    part.x = min(part.x + min(ns, kClamp), kClamp);
+                    part.y = min(part.y + min(tree, kClamp), kClamp);
+                }
+            block_exclusive_scan3<NT>(part, s_scan, &tot);
+        }
     const uint32_t prop_tile = tile_for(tot.x), old_tile = old_tile_for(tot.y);
+    const int sh_a = __ffs(prop_tile) - 1, sh_o = __ffs(old_tile) - 1;  // tile sizes are powers of two
     // pass 2: tiles per slot and their exclusive prefixes
     uint3 carry = make_uint3(0u, 0u, 0u);
     for(int base = 0; base < n; base += NT)
@@ -301,8 +318,8 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
             uint32_t ta = 0, tc = 0, told = 0;
             if(run)
                 {
-                    ta = (ns + prop_tile - 1) / prop_tile;
-                    told = (tree + old_tile - 1) / old_tile;
+                    ta = (ns + prop_tile - 1) >> sh_a;
+                    told = (tree + old_tile - 1) >> sh_o;
                     tc = told + (ns + kTileC - 1) / kTileC;
                 }
             uint3 sum;
@@ -740,6 +757,9 @@ __device__ inline void finalize_query(const QueryParams& p, QueryState& st, Sche
     plan_samples_vals(cap, spn, tree, react_total + w_total, &spe, &n_samples);
     st.spe = spe;
     st.n_samples = n_samples;
+    // the next schedule's totals (it sizes the tiles from them)
+    atomicAdd(&sched->next_samples, (unsigned long long)n_samples);
+    atomicAdd(&sched->next_tree, (unsigned long long)tree);
 }
 
 // Copies one sample row (written by the propagate kernel, read-only here)

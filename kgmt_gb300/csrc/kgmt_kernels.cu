@@ -550,23 +550,21 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
                     const uint32_t done = atomicAdd(&st.tiles_done, 1u);
                     // the block is free now: its next ticket, in flight with the count
                     next = gridDim.x + atomicAdd(&sched->ticket_c, 1u);
-                    if(done == n_tiles - 1)
-                        {
-                            __threadfence();
-                            st.f_accept = s_fa;
-                            finalize_query(p, st, sched);
-                            s_fin = 1;
-                        }
+                    if(done == n_tiles - 1) s_fin = 1;
                 }
             __syncthreads();
             if(s_fin)
                 {
-                    // every tile of this query is done: count it finalised,
-                    // then clear its look-back words for the next iteration
-                    // (nothing in this kernel reads them again, and the next
-                    // append launch sees the stores: no fence on the path)
+                    // every tile of this query is done: thread 0 finalises it
+                    // and counts it finalised while the other threads clear
+                    // its look-back words for the next iteration (nothing in
+                    // this kernel reads them again, and the next append
+                    // launch sees the stores: no fence on the path)
                     if(threadIdx.x == 0)
                         {
+                            __threadfence();
+                            st.f_accept = s_fa;
+                            finalize_query(p, st, sched);
                             __threadfence();
                             const uint32_t f = atomicAdd(&sched->finalized, 1u);
                             if(f == sched->running - 1) s_glob = 1;
@@ -579,7 +577,7 @@ __global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __
             if(s_glob)
                 {
                     __threadfence();
-                    compute_schedule(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
+                    compute_schedule<kAppendThreads, true>(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
                 }
             __syncthreads();
         }

@@ -190,6 +190,10 @@ struct Sched {
     uint32_t pair_samples;  // iterations with at least this many samples use kPropPer samples per thread
     uint32_t n_sms;         // SMs of the device: smaller iterations use smaller tiles, about one per SM
     uint32_t old_tile;      // old nodes per re-activation tile this iteration: kTileOld or kTileOldSmall
+    // samples and tree nodes of the queries still running, summed by this
+    // iteration's finalisers for the schedule of the next one
+    unsigned long long next_samples;
+    unsigned long long next_tree;
     // mapped pinned host word that mirrors `running` (or null): the host polls
     // it without a copy in the stream between graph replays
     uint32_t* host_running;
