@@ -375,7 +375,10 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
         }
 }
 
-__global__ void __launch_bounds__(kAppendThreads) k_append(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
+// eight blocks per SM (32 registers; the kernel waits on loads, scans and
+// look-back, so more tiles in flight hide more latency: the mixed batch
+// +4 %, the double-integrator batch unchanged)
+__global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams* __restrict__ P, QueryState* S, Sched* sched,
                                                            uint32_t* tile_a_base, uint32_t* tile_c_base, uint32_t* tile_c_old)
 {
     __shared__ uint32_t scratch[34];
