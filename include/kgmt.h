@@ -193,10 +193,28 @@ KGMT_API kgmt_status kgmt_batch_get_stats(kgmt_batch* b, kgmt_batch_stats* out);
 /* tree of query i of the last batch (host copy) */
 KGMT_API kgmt_status kgmt_batch_copy_tree(kgmt_batch* b, uint32_t i, float* h_samples, int32_t* h_parents, float* h_costs, uint32_t max_nodes);
 KGMT_API kgmt_status kgmt_batch_copy_path(kgmt_batch* b, uint32_t i, float* h_rows, uint32_t max_rows, uint32_t* n_rows);
-/* picks the propagate block size for a representative batch (sweeps 64..512) */
+/* picks the propagate block size for a representative batch (sweeps 128, 256, 512) */
 KGMT_API kgmt_status kgmt_batch_autotune(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits, const float* h_goals,
                                 const float* h_obstacles, const uint32_t* obs_offset, const uint32_t* obs_count,
                                 uint32_t* best_block);
+
+typedef struct kgmt_autotune_result {
+    uint32_t propagate_block;  /* chosen block size (now the batch's)                        */
+    uint32_t samples_per_node; /* chosen samples per expanded node: set it in the configs     */
+    float queries_per_s;       /* of the chosen pair (host clock around kgmt_plan_batch)      */
+    float success_rate;        /* of the chosen pair                                          */
+    float base_queries_per_s;  /* the configs as given, block 256                             */
+    float base_success_rate;
+} kgmt_autotune_result;
+
+/* sweeps the propagate block size (128, 256, 512) and the samples per
+   expanded node (2, 4, 8, 16) on a representative batch and keeps the pair
+   with the most queries/s among those whose success rate is at least 95 % of
+   the configs' own (samples per node changes the plans, so the caller
+   decides whether to adopt it: it is returned, not written into cfgs) */
+KGMT_API kgmt_status kgmt_batch_autotune_full(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits,
+                                              const float* h_goals, const float* h_obstacles, const uint32_t* obs_offset,
+                                              const uint32_t* obs_count, kgmt_autotune_result* out);
 
 /* ---- served: continuous batching with memory-based admission ---- */
 typedef struct kgmt_server_options {

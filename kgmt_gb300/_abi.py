@@ -62,6 +62,14 @@ class KgmtBatchStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class KgmtAutotuneResult(C.Structure):
+    _fields_ = [("propagate_block", C.c_uint32), ("samples_per_node", C.c_uint32), ("queries_per_s", C.c_float),
+                ("success_rate", C.c_float), ("base_queries_per_s", C.c_float), ("base_success_rate", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class KgmtServerOptions(C.Structure):
     _fields_ = [("max_slots", C.c_uint32), ("memory_budget", C.c_uint64), ("iters_per_step", C.c_uint32),
                 ("propagate_block", C.c_uint32)]
@@ -105,6 +113,7 @@ SIGNATURES = {
     "kgmt_batch_copy_tree": (_i32, [_vp, _u32, _vp, _vp, _vp, _u32]),
     "kgmt_batch_copy_path": (_i32, [_vp, _u32, _vp, _u32, _u32p]),
     "kgmt_batch_autotune": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, _u32p]),
+    "kgmt_batch_autotune_full": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, C.POINTER(KgmtAutotuneResult)]),
     "kgmt_server_create": (_i32, [C.POINTER(KgmtServerOptions), _vp, C.POINTER(_vp)]),
     "kgmt_server_destroy": (None, [_vp]),
     "kgmt_server_submit": (_i32, [_vp, _cfgp, _vp, _vp, _vp, _u32, C.POINTER(C.c_uint64)]),

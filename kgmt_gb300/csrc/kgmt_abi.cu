@@ -495,6 +495,60 @@ extern "C" kgmt_status kgmt_batch_autotune(kgmt_batch* b, uint32_t n, const kgmt
     return KGMT_OK;
 }
 
+extern "C" kgmt_status kgmt_batch_autotune_full(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs, const float* h_inits,
+                                                const float* h_goals, const float* h_obstacles, const uint32_t* obs_offset,
+                                                const uint32_t* obs_count, kgmt_autotune_result* out)
+{
+    RETURN_IF(!b || !cfgs || !out, KGMT_ERR_INVALID_ARG, "kgmt_batch_autotune_full: NULL argument");
+    RETURN_IF(n == 0, KGMT_ERR_INVALID_ARG, "kgmt_batch_autotune_full: empty batch");
+    std::vector<kgmt_config> c(cfgs, cfgs + n);
+    std::vector<kgmt_result> res(n);
+    // one warm-up and one timed plan of the batch at (block, samples per node; 0 = as given)
+    auto trial = [&](uint32_t blk, uint32_t spn, double* qps, double* succ) -> kgmt_status {
+        CHECK_ST(b->eng.set_prop_block(blk));
+        for(uint32_t i = 0; i < n; ++i) c[i].samples_per_node = spn ? spn : cfgs[i].samples_per_node;
+        CHECK_ST(kgmt_plan_batch(b, n, c.data(), h_inits, h_goals, h_obstacles, obs_offset, obs_count, res.data()));
+        const auto t0 = std::chrono::steady_clock::now();
+        CHECK_ST(kgmt_plan_batch(b, n, c.data(), h_inits, h_goals, h_obstacles, obs_offset, obs_count, res.data()));
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        uint32_t ok = 0;
+        for(uint32_t i = 0; i < n; ++i) ok += res[i].status == KGMT_QUERY_SUCCESS ? 1u : 0u;
+        *qps = t > 0.0 ? n / t : 0.0;
+        *succ = (double)ok / n;
+        return KGMT_OK;
+    };
+    double base_qps = 0.0, base_succ = 0.0;
+    CHECK_ST(trial(256, 0, &base_qps, &base_succ));
+    uint32_t best_blk = 256, best_spn = cfgs[0].samples_per_node;
+    double best_qps = -1.0, best_succ = base_succ;
+    const uint32_t blocks[3] = {128, 256, 512};
+    const uint32_t spns[4] = {2, 4, 8, 16};
+    for(uint32_t spn : spns)
+        for(uint32_t blk : blocks)
+            {
+                double qps = 0.0, succ = 0.0;
+                CHECK_ST(trial(blk, spn, &qps, &succ));
+                if(succ >= 0.95 * base_succ && qps > best_qps)
+                    {
+                        best_qps = qps, best_succ = succ;
+                        best_blk = blk, best_spn = spn;
+                    }
+            }
+    if(best_qps < 0.0)
+        {
+            // nothing kept the success rate: the configs as given
+            best_qps = base_qps;
+        }
+    CHECK_ST(b->eng.set_prop_block(best_blk));
+    out->propagate_block = best_blk;
+    out->samples_per_node = best_spn;
+    out->queries_per_s = (float)best_qps;
+    out->success_rate = (float)best_succ;
+    out->base_queries_per_s = (float)base_qps;
+    out->base_success_rate = (float)base_succ;
+    return KGMT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // server: continuous batching with memory-based admission
 // ---------------------------------------------------------------------------

@@ -203,6 +203,20 @@ class BatchPlanner:
                                             off.ctypes.data, cnt.ctypes.data, C.byref(best)))
         return best.value
 
+    def autotune_full(self, cfgs, inits, goals, obstacles, obs_offset, obs_count) -> dict:
+        """Block size x samples per node sweep (kgmt_batch_autotune_full): the
+        batch keeps the chosen block size; the chosen samples per node is
+        returned for the caller to put into its configs."""
+        n = len(cfgs)
+        carr = pack_configs(cfgs)
+        inits, goals, obstacles = _f32(inits), _f32(goals), _f32(obstacles)
+        off = np.ascontiguousarray(obs_offset, np.uint32)
+        cnt = np.ascontiguousarray(obs_count, np.uint32)
+        out = _abi.KgmtAutotuneResult()
+        check(self._lib.kgmt_batch_autotune_full(self._h, n, carr, inits.ctypes.data, goals.ctypes.data, obstacles.ctypes.data,
+                                                 off.ctypes.data, cnt.ctypes.data, C.byref(out)))
+        return out.as_dict()
+
 
 class Server:
     """Continuous batching with memory-based admission."""

@@ -367,6 +367,35 @@ def test_block_size_does_not_change_results(block):
         [(r["tree_size"], r["goal_index"], r["iterations"]) for r in other]
 
 
+def test_autotuner_block_and_samples_per_node():
+    """kgmt_batch_autotune picks a block size the batch then keeps, and the
+    results do not depend on it; kgmt_batch_autotune_full sweeps block size x
+    samples per node and keeps the success rate within 95 % of the configs'
+    own (its pick, planned again, gives that success rate)."""
+    from kgmt_gb300.planner import BatchPlanner
+    qs = W.double_integrator_batch(16, seed=12, tree_capacity=20_000)
+    cfgs = [q.config for q in qs]
+    inits, goals, obs, offs, cnts = W.pack_queries(qs)
+    b = BatchPlanner(len(qs))
+    base = b.plan(cfgs, inits, goals, obs, offs, cnts)
+    blk = b.autotune(cfgs, inits, goals, obs, offs, cnts)
+    assert blk in (128, 256, 512)
+    again = b.plan(cfgs, inits, goals, obs, offs, cnts)
+    assert [(r["tree_size"], r["goal_index"]) for r in again] == [(r["tree_size"], r["goal_index"]) for r in base]
+    t = b.autotune_full(cfgs, inits, goals, obs, offs, cnts)
+    assert t["propagate_block"] in (128, 256, 512) and t["samples_per_node"] in (2, 4, 8, 16)
+    assert t["success_rate"] >= 0.95 * t["base_success_rate"] - 1e-6
+    assert t["queries_per_s"] > 0 and t["base_queries_per_s"] > 0
+    tuned = [c.replace(samples_per_node=t["samples_per_node"]) for c in cfgs]
+    res = b.plan(tuned, inits, goals, obs, offs, cnts)
+    assert abs(sum(r["status"] == 1 for r in res) / len(qs) - t["success_rate"]) < 1e-6
+    # the tuned batch is still the oracle's
+    refs = O.plan_batch([type(q)(c, q.init, q.goal, q.obstacles) for q, c in zip(qs, tuned)])
+    for r, ref in zip(res, refs):
+        assert (r["status"], r["tree_size"], r["goal_index"]) == (ref["status"], ref["tree_size"], ref["goal_index"])
+    b.close()
+
+
 def test_server_results_same_alone_and_in_mix():
     from kgmt_gb300.planner import Server
     qs = W.double_integrator_batch(12, seed=6, tree_capacity=20_000)
