@@ -415,6 +415,42 @@ __device__ __forceinline__ bool propagate_model(const QueryParams& p, const Grid
     else return propagate_di(p, grid, x0, u, obs, n_obs, x1, cnt);
 }
 
+// rows of D floats: with D even every row starts 8-byte aligned (row
+// buffers are 256-byte aligned), so they move as float2 pairs
+template <int D>
+__device__ __forceinline__ void load_row_ro(const float* __restrict__ src, float* r)
+{
+    if constexpr(D % 2 == 0)
+        {
+#pragma unroll
+            for(int c = 0; c < D / 2; ++c)
+                {
+                    const float2 v = __ldg((const float2*)src + c);
+                    r[2 * c] = v.x, r[2 * c + 1] = v.y;
+                }
+        }
+    else
+        {
+#pragma unroll
+            for(int c = 0; c < D; ++c) r[c] = __ldg(src + c);
+        }
+}
+
+template <int D>
+__device__ __forceinline__ void store_row(float* dst, const float* r)
+{
+    if constexpr(D % 2 == 0)
+        {
+#pragma unroll
+            for(int c = 0; c < D / 2; ++c) ((float2*)dst)[c] = make_float2(r[2 * c], r[2 * c + 1]);
+        }
+    else
+        {
+#pragma unroll
+            for(int c = 0; c < D; ++c) dst[c] = r[c];
+        }
+}
+
 // A sample's eight uniforms come from two Philox blocks, (s, itr, 0, 0) and
 // (s, itr, 0, 1): controls first, then the step draw, then the accept draw.
 // The block holding the step draw ("key block": the first for three
@@ -443,9 +479,7 @@ __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const P
     constexpr int D = ModelDims<MODEL>::D;
     const uint32_t e = s / c.spe;
     const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
-    const float* src = p.tree + (size_t)par * D;
-#pragma unroll
-    for(int j = 0; j < D; ++j) x0[j] = __ldg(src + j);
+    load_row_ro<D>(p.tree + (size_t)par * D, x0);
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
     constexpr bool four = ModelDims<MODEL>::NC == 4;
     const U4 other = philox4x32_10(s, c.itr, 0u, four ? 0u : 1u, k0, k1);
@@ -483,9 +517,7 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
                     marks = p.marks[r1];
                     score = p.score[r1];
                 }
-            float* dst = p.us + (size_t)s * D;
-#pragma unroll
-            for(int j = 0; j < D; ++j) dst[j] = x1[j];
+            store_row<D>(p.us + (size_t)s * D, x1);
             p.up[s] = (int32_t)par;
             p.ur1[s] = r1;
             if(ok)
@@ -761,10 +793,8 @@ template <int D>
 __device__ __forceinline__ float append_row_d(const QueryParams& p, const float* src, float* dst)
 {
     float r[D];
-#pragma unroll
-    for(int c = 0; c < D; ++c) r[c] = __ldg(src + c);
-#pragma unroll
-    for(int c = 0; c < D; ++c) dst[c] = r[c];
+    load_row_ro<D>(src, r);
+    store_row<D>(dst, r);
     return goal_distance(p, r);
 }
 
