@@ -173,8 +173,7 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_ob
     L.rep_new = aligned(cur, T * 4);
     L.us = aligned(cur, T * D * 4);
     L.up = aligned(cur, T * 4);
-    L.ur1 = aligned(cur, T * 4);
-    L.uflag = aligned(cur, T);
+    L.ur1f = aligned(cur, T * 4);
     L.counter = aligned(cur, R1 * 4);
     L.valid = aligned(cur, R1 * 4);
     L.score = aligned(cur, R1 * 4);
@@ -287,8 +286,7 @@ QueryParams make_params(const kgmt_config& c, const float* init, const float* go
     p.rep_new = (uint32_t*)(chunk + L.rep_new);
     p.us = (float*)(chunk + L.us);
     p.up = (int32_t*)(chunk + L.up);
-    p.ur1 = (int32_t*)(chunk + L.ur1);
-    p.uflag = (uint8_t*)(chunk + L.uflag);
+    p.ur1f = (uint32_t*)(chunk + L.ur1f);
     p.counter = (int32_t*)(chunk + L.counter);
     p.valid = (int32_t*)(chunk + L.valid);
     p.score = (float*)(chunk + L.score);

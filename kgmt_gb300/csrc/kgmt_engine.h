@@ -42,7 +42,7 @@ class DeviceArena {
 };
 
 struct QueryLayout {
-    size_t tree, parent, cost, node_r1, rep_old, rep_new, us, up, ur1, uflag;
+    size_t tree, parent, cost, node_r1, rep_old, rep_new, us, up, ur1f;
     size_t counter, valid, score, marks, newmarks, tiles_old, tiles_slot, path, grid_meta, grid_start, grid_items, obstacles;
     size_t total;
     uint32_t tiles_per_chain;

@@ -519,13 +519,13 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
                 }
             store_row<D>(p.us + (size_t)s * D, x1);
             p.up[s] = (int32_t)par;
-            p.ur1[s] = r1;
             if(ok)
                 {
                     const bool fresh = (marks & bit) == 0ull;
                     acc = (u[NC + 1] < score) || fresh;
                 }
-            p.uflag[s] = acc ? 1 : 0;
+            // region and accept flag in one word (region ids are below 2^31)
+            p.ur1f[s] = (uint32_t)r1 | (acc ? 0x80000000u : 0u);
         }
     // histogram updates (KGMT.cu:250-253): counter over all samples, valid
     // count and the fine-cell bit over the valid ones; one fire-and-forget L2

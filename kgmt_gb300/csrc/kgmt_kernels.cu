@@ -487,16 +487,28 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                     const uint32_t s0 = lts * kTileC + threadIdx.x * kAppendPer;
                     const uint32_t ns = st.n_samples;
                     uint32_t acc_bits = 0, ca = 0, cw = 0;
-                    // flags and regions are read together, then the accepted
-                    // samples' valid counts: two round trips, not three
+                    // region-and-flag words of the thread's samples (s0 is a
+                    // multiple of 4: one 16-byte load), then the accepted
+                    // samples' valid counts: two round trips
+                    static_assert(kAppendPer == 4, "one 16-byte load of four region-and-flag words");
                     uint32_t fl[kAppendPer];
                     int32_t rg[kAppendPer];
+                    uint32_t rf[kAppendPer];
+                    if(s0 + 3 < ns)
+                        {
+                            const uint4 v = *(const uint4*)(p.ur1f + s0);
+                            rf[0] = v.x, rf[1] = v.y, rf[2] = v.z, rf[3] = v.w;
+                        }
+                    else
+                        {
+#pragma unroll
+                            for(int j = 0; j < kAppendPer; ++j) rf[j] = s0 + j < ns ? p.ur1f[s0 + j] : 0u;
+                        }
 #pragma unroll
                     for(int j = 0; j < kAppendPer; ++j)
                         {
-                            const uint32_t s = s0 + j;
-                            fl[j] = s < ns ? p.uflag[s] : 0u;
-                            rg[j] = s < ns ? p.ur1[s] : 0;
+                            fl[j] = rf[j] >> 31;
+                            rg[j] = (int32_t)(rf[j] & 0x7FFFFFFFu);
                         }
                     uint32_t w[kAppendPer];
 #pragma unroll

@@ -127,8 +127,7 @@ struct QueryParams {
     uint32_t* rep_new;    // [capacity] new nodes, each repeated 15 or 1 times
     float* us;            // [capacity][sample_dim] unexplored samples
     int32_t* up;          // [capacity] parent of each sample
-    int32_t* ur1;         // [capacity] region of each sample
-    uint8_t* uflag;       // [capacity] sample joins the tree
+    uint32_t* ur1f;       // [capacity] region of each sample; top bit: the sample joins the tree
     int32_t* counter;     // [regions] samples per region          (d_counterArray_)
     int32_t* valid;       // [regions] valid samples per region    (d_validCounterArray_)
     float* score;         // [regions]                              (d_vertexScoreArray_)
