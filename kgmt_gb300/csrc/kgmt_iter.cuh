@@ -508,23 +508,21 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
             const CellIds cid = cell_ids(p, x1);
             r1 = cid.r1;
             bit = 1ull << cid.r2;
-            // the region's marks and score are loaded before the row stores
-            // (which the compiler must otherwise keep ahead of them)
-            uint64_t marks = 0ull;
-            float score = 0.0f;
             if(ok)
                 {
-                    marks = p.marks[r1];
-                    score = p.score[r1];
-                }
-            store_row<D>(p.us + (size_t)s * D, x1);
-            p.up[s] = (int32_t)par;
-            if(ok)
-                {
+                    const uint64_t marks = p.marks[r1];
+                    const float score = p.score[r1];
                     const bool fresh = (marks & bit) == 0ull;
                     acc = (u[NC + 1] < score) || fresh;
                 }
-            // region and accept flag in one word (region ids are below 2^31)
+            // only a sample that joins the tree is read again (by the append
+            // kernel): its row and parent; every sample's region and accept
+            // flag, in one word (region ids are below 2^31)
+            if(acc)
+                {
+                    store_row<D>(p.us + (size_t)s * D, x1);
+                    p.up[s] = (int32_t)par;
+                }
             p.ur1f[s] = (uint32_t)r1 | (acc ? 0x80000000u : 0u);
         }
     // histogram updates (KGMT.cu:250-253): counter over all samples, valid
