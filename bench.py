@@ -137,13 +137,14 @@ class ClockSampler:
 # DRAM bytes (read + write) per k_propagate launch on this workload, from one
 # ncu capture of a planning step (dram__bytes_read.sum + dram__bytes_write.sum
 # summed over its 132 propagate launches, --cache-control none --clock-control
-# none): 694 MB read + 2096 MB written.  The live algorithmic bytes per launch
-# (sample rows, parent, region and flag written; parent rows and frontier
-# indices read) are reported beside it.
-PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (694.43e6 + 2096.29e6) / 132
-# algorithmic bytes per double-integrator sample: row (10 floats), parent,
-# region and flag written; the parent's row and its frontier index read
-PROPAGATE_BYTES_PER_SAMPLE = 10 * 4 + 4 + 4 + 1 + 10 * 4 + 4
+# none): 551 MB read + 592 MB written.  The live algorithmic bytes per launch
+# are reported beside it.
+PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (551.45e6 + 592.36e6) / 132
+# algorithmic bytes of the double-integrator propagate: per sample the
+# frontier index and the parent's row (10 floats) read and the region-and-
+# accept word written; per sample that joins the tree also its row and parent
+PROPAGATE_BYTES_PER_SAMPLE = 4 + 10 * 4 + 4
+PROPAGATE_BYTES_PER_ACCEPTED = 10 * 4 + 4
 
 
 # ---------------------------------------------------------------------------
@@ -376,7 +377,8 @@ def run_ours(args) -> None:
                          "unit": "T FP32 lane-ops/s", "frac": achieved / fp32_peak,
                          "traffic": PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH,
                          "traffic_unit": "DRAM bytes per launch (ncu capture of this workload)",
-                         "algorithmic_bytes_per_launch": st["samples"] * PROPAGATE_BYTES_PER_SAMPLE
+                         "algorithmic_bytes_per_launch": (st["samples"] * PROPAGATE_BYTES_PER_SAMPLE
+                                                          + sum(r["tree_size"] - 1 for r in last) * PROPAGATE_BYTES_PER_ACCEPTED)
                          / max(1, st["launches_propagate"]),
                          "peak_source": "measured: cuBLAS SGEMM 8192^3 (TF32 off) FLOP/s / 2",
                          "avg_launch_ms": prop_ms_avg, "launches": st["launches_propagate"],
