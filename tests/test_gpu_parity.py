@@ -347,6 +347,27 @@ def test_batch_matches_oracle_and_plain():
         assert np.array_equal(s[:n].view(np.uint32), alone[1].view(np.uint32))
 
 
+def test_large_batch_matches_oracle():
+    """A batch large enough for the big-iteration paths: two samples per
+    thread in the propagate tiles (iterations of more than twice the resident
+    threads' samples) and 4096-node re-activation tiles (trees filling more
+    large tiles than there are SMs), then the small-tile tail of its last
+    queries; every query as the oracle plans it."""
+    qs = W.double_integrator_batch(96, n_obstacles=50, seed=21, tree_capacity=50_000)
+    b, res = _batch(qs)
+    refs = O.plan_batch(qs)
+    for i, (r, ref) in enumerate(zip(res, refs)):
+        for k in ("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn"):
+            assert r[k] == ref[k], (i, k, r[k], ref[k])
+    for i in (0, 50, 95):
+        s, par, c = b.copy_tree(i)
+        n = res[i]["tree_size"]
+        ref = O.plan(qs[i])
+        assert np.array_equal(par[:n], ref["parents"])
+        assert np.array_equal(s[:n].view(np.uint32), ref["samples"].view(np.uint32))
+    b.close()
+
+
 def test_batch_heterogeneous_matches_oracle():
     qs = W.mixed_batch(24, seed=2, capacity_scale=0.1)
     for q in qs:
