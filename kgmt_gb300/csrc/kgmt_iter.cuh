@@ -58,6 +58,17 @@ __device__ __forceinline__ unsigned long long globaltimer()
     return t;
 }
 
+// the last-one-in count of a tile or query: a release add at GPU scope
+// (everything this thread wrote, and what the block wrote before the last
+// __syncthreads, is visible to whoever reads the count afterwards and
+// fences) -- lighter than a full fence followed by a relaxed add
+__device__ __forceinline__ uint32_t atomic_add_release(uint32_t* p, uint32_t v)
+{
+    uint32_t old;
+    asm volatile("atom.add.release.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 // programmatic dependent launch: the kernel that follows in the stream may
 // be scheduled once every block of this one has called pdl_trigger (or
 // exited); pdl_wait blocks until the kernel before this one has completed

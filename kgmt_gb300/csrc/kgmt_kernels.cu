@@ -358,9 +358,8 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                     if(s_sh.acc) atomicAdd(&st.n_next, s_sh.acc);
                     if(s_sh.steps) atomicAdd(&st.steps, (unsigned long long)s_sh.steps);
                     if(s_sh.tests) atomicAdd(&st.tests, (unsigned long long)s_sh.tests);
-                    __threadfence();
                     const uint32_t n_tiles = bases.base[q + 1] - bases.base[q];
-                    if(atomicAdd(&st.prop_done, 1u) == n_tiles - 1) s_last = 1;
+                    if(atomic_add_release(&st.prop_done, 1u) == n_tiles - 1) s_last = 1;
                     t = t_next;
                     s_tile = (int)t;
                 }
@@ -560,9 +559,8 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
             __syncthreads();
             if(threadIdx.x == 0)
                 {
-                    __threadfence();
                     const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
-                    const uint32_t done = atomicAdd(&st.tiles_done, 1u);
+                    const uint32_t done = atomic_add_release(&st.tiles_done, 1u);
                     // the block is free now: its next ticket, in flight with the count
                     next = gridDim.x + atomicAdd(&sched->ticket_c, 1u);
                     if(done == n_tiles - 1) s_fin = 1;
@@ -580,8 +578,7 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                             __threadfence();
                             st.f_accept = s_fa;
                             finalize_query(p, st, sched);
-                            __threadfence();
-                            const uint32_t f = atomicAdd(&sched->finalized, 1u);
+                            const uint32_t f = atomic_add_release(&sched->finalized, 1u);
                             if(f == sched->running - 1) s_glob = 1;
                         }
                     const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
