@@ -649,8 +649,20 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
 // regions scored, lane l of kScoreLanes sums regions l, l+256, ... in order,
 // then a halving tree over the lanes.  Histograms and marks were updated by
 // other blocks' atomics in this kernel: read past L1.
+// The fields of QueryParams the scores use, held in registers.
+struct ScoreParams
+{
+    int32_t* counter;
+    int32_t* valid;
+    float* score;
+    uint64_t* marks;
+    uint64_t* newmarks;
+    uint32_t regions, fine_cells;
+    float epsilon, cell_volume;
+};
+
 template <int NT>
-__device__ void update_scores(const QueryParams& p, QueryState& st, float* lanes)
+__device__ void update_scores(const ScoreParams& p, QueryState& st, float* lanes)
 {
     const float F = (float)p.fine_cells;
     constexpr int U = 4;  // regions whose loads are issued together

@@ -367,7 +367,8 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
             if(s_last)
                 {
                     __threadfence();
-                    update_scores<NT>(s_p, S[q], s_lanes);
+                    const ScoreParams sp{s_p.counter, s_p.valid, s_p.score, s_p.marks, s_p.newmarks, s_p.regions, s_p.fine_cells, s_p.epsilon, s_p.cell_volume};
+                    update_scores<NT>(sp, S[q], s_lanes);
                 }
             t = (uint32_t)s_tile;
             __syncthreads();
