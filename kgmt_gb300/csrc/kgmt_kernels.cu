@@ -579,8 +579,16 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                             __threadfence();
                             st.f_accept = s_fa;
                             finalize_query(p, st, sched);
-                            const uint32_t f = atomic_add_release(&sched->finalized, 1u);
-                            if(f == sched->running - 1) s_glob = 1;
+                            const uint32_t running = sched->running;
+                            if(running == 1u)
+                                {
+                                    // the only running query: its finaliser is
+                                    // the last, and no other block's results
+                                    // are left to acquire (2: no block fence)
+                                    __threadfence();
+                                    s_glob = 2;
+                                }
+                            else if(atomic_add_release(&sched->finalized, 1u) == running - 1u) s_glob = 1;
                         }
                     const uint32_t n_tiles = cbase.base[q + 1] - cbase.base[q];
                     for(uint32_t i = threadIdx.x; i < n_old; i += kAppendThreads) p.tiles_old[i] = 0ull;
@@ -589,7 +597,7 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                 }
             if(s_glob)
                 {
-                    __threadfence();
+                    if(s_glob == 1) __threadfence();
                     compute_schedule<kAppendThreads, true>(P, S, sched, tile_a_base, tile_c_base, tile_c_old);
                 }
             __syncthreads();
