@@ -251,7 +251,8 @@ struct StepCells {
 
 __device__ __forceinline__ StepCells start_cells(const QueryParams& P, float x, float y, float z)
 {
-    return {grid_cell(P, x), grid_cell(P, y), grid_cell(P, z), (x == x) & (y == y) & (z == z)};
+    const bool ok = (x == x) & (y == y) & (z == z);
+    return {grid_cell(P, x), grid_cell(P, y), grid_cell(P, z), ok};
 }
 
 // true when the step box [a, b] (per-axis min/max) hits no obstacle.  The grid
