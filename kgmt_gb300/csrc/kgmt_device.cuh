@@ -543,7 +543,9 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
     sincos_portable(phi, sphi, cphi);
     sincos_portable(theta, sth, cth);
     sincos_portable(psi, spsi, cpsi);
-    const float tth = sth / cth;
+    // the two terms over cos(theta) share one division
+    const float icth = 1.0f / cth;
+    const float tth = sth * icth;
     const float g = P.gravity;
     const float sps = sphi * sth, cps = cphi * sth;
     d[0] = fmaf(fmaf(cps, cpsi, sphi * spsi), ww, fmaf(fmaf(sps, cpsi, -(cphi * spsi)), vv, (cth * cpsi) * uu));
@@ -552,7 +554,7 @@ __device__ __forceinline__ void quad_ode(const QueryParams& P, const float* s, f
     const float qr = fmaf(q, sphi, r * cphi);
     d[3] = fmaf(qr, tth, p);
     d[4] = fmaf(q, cphi, -(r * sphi));
-    d[5] = qr / cth;
+    d[5] = qr * icth;
     const float xyz = (-P.nu) * sqrtf(fmaf(ww, ww, fmaf(vv, vv, uu * uu)));
     const float mx = P.mass_inv * xyz;
     d[6] = fmaf(mx, uu, fmaf(-g, sth, fmaf(r, vv, -(q * ww))));

@@ -43,9 +43,9 @@ constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-a
 // static FP32 lane-operation counts per RK4 step, from the code in
 // kgmt_device.cuh (a multiply, add, fused multiply-add, divide or compare is
 // one; the quadrotor's portable sine/cosine counted as the operations it is
-// made of: 4 ode evaluations of ~139, stage and update combinations, checks)
+// made of: 4 ode evaluations of ~140, stage and update combinations, checks)
 constexpr uint32_t kOpsPerStepDI = 81;
-constexpr uint32_t kOpsPerStepQuad = 658;
+constexpr uint32_t kOpsPerStepQuad = 662;
 // Dubins airplane: 4 portable sine/cosine pairs (~26 each: reduction, two
 // polynomials, quadrant selection), 4 attitude offsets, 12 stage products,
 // 23 for the three position sums, 3 updates, 10 compares

@@ -472,7 +472,9 @@ static void quad_ode_f(const ko_config* c, const float* s, const quad_ctrl_f* u,
     ko_sincosf(phi, &sphi, &cphi);
     ko_sincosf(theta, &sth, &cth);
     ko_sincosf(psi, &spsi, &cpsi);
-    float tth = sth / cth;
+    /* the two terms over cos(theta) share one division, as on the device */
+    const float icth = 1.0f / cth;
+    float tth = sth * icth;
     const float g = c->gravity;
     const float sps = sphi * sth, cps = cphi * sth;
     d[0] = fmaf(fmaf(cps, cpsi, sphi * spsi), ww, fmaf(fmaf(sps, cpsi, -(cphi * spsi)), vv, (cth * cpsi) * uu));
@@ -481,7 +483,7 @@ static void quad_ode_f(const ko_config* c, const float* s, const quad_ctrl_f* u,
     float qr = fmaf(q, sphi, r * cphi);
     d[3] = fmaf(qr, tth, p);
     d[4] = fmaf(q, cphi, -(r * sphi));
-    d[5] = qr / cth;
+    d[5] = qr * icth;
     float xyz = (-c->nu) * sqrtf(fmaf(ww, ww, fmaf(vv, vv, uu * uu)));
     float mx = c->mass_inv * xyz;
     d[6] = fmaf(mx, uu, fmaf(-g, sth, fmaf(r, vv, -(q * ww))));
