@@ -440,3 +440,108 @@ def test_server_results_same_alone_and_in_mix():
     for i, ref in enumerate(refs):
         for k in ("status", "iterations", "tree_size", "goal_index", "samples_drawn"):
             assert got[i][k] == ref[k], (i, k, got[i][k], ref[k])
+
+
+# ---------------------------------------------------------------------------
+# The reference's own configurations at full size, too large for the oracle
+# to plan in seconds: properties that hold whatever the size.
+# ---------------------------------------------------------------------------
+def reconstruct_uniforms(cfg, rows):
+    """The uniforms that give a tree row's controls and step count: each
+    control c = u_min + u * (u_max - u_min) in unfused FP32 (as the kernels
+    and the oracle compute it) inverted, then moved by ulps until it gives c
+    back exactly; the step draw centred on its count."""
+    NC = 4 if cfg.sample_dim == 17 else 3
+    D = cfg.sample_dim
+    n = rows.shape[0]
+    u = np.full((n, 8), 0.5, np.float32)
+    umin = np.asarray(cfg.u_min, np.float32)[:NC]
+    span = (np.asarray(cfg.u_max, np.float32)[:NC] - umin).astype(np.float32)
+    live = span > 0
+    ctrl = rows[:, D - 1 - NC:D - 1].astype(np.float32)
+    uc = ((ctrl.astype(np.float64) - umin) / np.where(live, span, 1.0)).astype(np.float32)
+    uc = np.where(live, uc, np.float32(0.5))
+    for _ in range(8):
+        c = umin + uc * span
+        uc = np.where(live & (c < ctrl), np.nextafter(uc, np.float32(2.0)), uc)
+        uc = np.where(live & (c > ctrl), np.nextafter(uc, np.float32(-1.0)), uc)
+    assert (~live | (umin + uc * span == ctrl)).all(), "a control no uniform gives"
+    u[:, :NC] = uc
+    k = np.rint(rows[:, D - 1].astype(np.float64) / cfg.step_size)
+    u[:, NC] = ((k - cfg.min_steps + 0.5) / (cfg.max_steps - cfg.min_steps + 1)).astype(np.float32)
+    return u
+
+
+def check_tree_properties(q, res, samples, parents, costs, path, n_edges=3000, seed=0):
+    cfg = q.config
+    D = cfg.sample_dim
+    n = res["tree_size"]
+    assert 1 <= n <= cfg.tree_capacity
+    S, P, C = samples[:n], parents[:n], costs[:n]
+    # every node but the root hangs off an earlier node
+    assert P[0] == -1
+    assert ((P[1:] >= 0) & (P[1:] < np.arange(1, n))).all()
+    # rows are finite, inside the workspace and the velocity bounds
+    assert np.isfinite(S).all()
+    assert ((S[:, :3] >= cfg.ws_min) & (S[:, :3] <= cfg.ws_max)).all()
+    vel = slice(3, 6) if D == 10 else slice(6, 9)
+    assert ((S[1:, vel] >= cfg.v_min) & (S[1:, vel] <= cfg.v_max)).all()
+    # durations are whole step counts within [min_steps, max_steps]
+    k = S[1:, D - 1] / np.float32(cfg.step_size)
+    assert np.allclose(k, np.rint(k), atol=1e-4)
+    assert ((np.rint(k) >= cfg.min_steps) & (np.rint(k) <= cfg.max_steps)).all()
+    # costs are the goal distances in the kernel's FP32 order (the root's is 0)
+    g = np.asarray(q.goal, np.float32)
+    d = [S[1:, j] - g[j] for j in range(3)]
+    ref_cost = np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])
+    assert C[0] == 0.0
+    assert np.array_equal(C[1:].view(np.uint32), ref_cost.astype(np.float32).view(np.uint32))
+    # a success ends in the goal ball, and its path is the parent chain
+    if res["status"] == 1:
+        gi = res["goal_index"]
+        assert 0 <= gi < n and C[gi] < cfg.goal_radius
+        chain = [gi]
+        while P[chain[-1]] >= 0:
+            chain.append(int(P[chain[-1]]))
+        assert res["path_len"] == len(chain)
+        assert np.array_equal(path.view(np.uint32), S[chain].view(np.uint32))
+    # edges re-propagated by the oracle's FP32 restatement from the parent
+    # with the child's controls and step count give the child bit for bit,
+    # collision-free; for the double integrator also within 1e-5 of FP64 (the
+    # quadrotor's Euler-angle kinematics make FP32 and FP64 part near
+    # theta = +-pi/2, where tan and 1/cos blow up: a property of the model)
+    rng = np.random.default_rng(seed)
+    kids = rng.choice(np.arange(1, n), size=min(n_edges, n - 1), replace=False)
+    u = reconstruct_uniforms(cfg, S[kids])
+    x32, valid32, _, _ = O.propagate_f32(cfg, S[P[kids]], u, q.obstacles)
+    assert valid32.all(), kids[valid32 == 0][:5]
+    assert np.array_equal(x32.view(np.uint32), S[kids].view(np.uint32)), kids[(x32 != S[kids]).any(axis=1)][:5]
+    if D == 10:
+        x1, valid = O.propagate_f64(cfg, S[P[kids]], u, q.obstacles)
+        tol = REL_TOL * np.maximum(np.abs(S[kids]), state_scales(cfg))
+        assert (np.abs(x1 - S[kids]) <= tol).all(), np.argwhere(np.abs(x1 - S[kids]) > tol)[:5]
+        for i in np.flatnonzero(valid == 0):
+            assert O.verdict_margin_f64(cfg, S[P[kids[i]]], u[i], q.obstacles) < 1e-6, kids[i]
+
+
+@pytest.mark.parametrize("which", ["di_single_T100k", "quad_T2M"])
+def test_full_size_single_query_properties(which):
+    """The single double-integrator query (T = 100k) and the large quadrotor
+    query (T = 2M, 8 samples per node, 200 boxes, 16^3 / 4^3 grid)."""
+    q = W.double_integrator_query(seed=4) if which == "di_single_T100k" else W.quadrotor_query(seed=2)
+    res, samples, parents, costs, path = plan_gpu(q)
+    assert res["status"] in (1, 2, 3), res
+    check_tree_properties(q, res, samples, parents, costs, path)
+
+
+def test_full_size_batch_properties():
+    """The 256-query double-integrator batch (50 boxes, T = 50k each): every
+    query's tree, checked on a sample of its queries including the slowest."""
+    qs = W.double_integrator_batch(256, n_obstacles=50, seed=1, tree_capacity=50_000)
+    b, res = _batch(qs)
+    slowest = int(np.argmax([r["iterations"] for r in res]))
+    for i in sorted({0, 1, 127, 255, slowest}):
+        s, p, c = b.copy_tree(i)
+        check_tree_properties(qs[i], res[i], s, p, c, b.copy_path(i), n_edges=1000, seed=i)
+    assert all(r["status"] == 1 for r in res)
+    b.close()
