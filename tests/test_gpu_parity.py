@@ -545,3 +545,21 @@ def test_full_size_batch_properties():
         check_tree_properties(qs[i], res[i], s, p, c, b.copy_path(i), n_edges=1000, seed=i)
     assert all(r["status"] == 1 for r in res)
     b.close()
+
+
+def test_full_size_mixed_batch_properties():
+    """The 1024-query mixed batch (half double integrator, half quadrotor;
+    5..1000 boxes, 8^3..32^3 grids, T 10k..500k): both models' trees, the
+    largest of each and the slowest queries among those checked."""
+    qs = W.mixed_batch(1024, seed=1)
+    b, res = _batch(qs)
+    pick = set()
+    for model_odd in (0, 1):  # even slots double integrator, odd ones quadrotor
+        idx = [i for i in range(len(qs)) if i % 2 == model_odd]
+        pick.add(max(idx, key=lambda i: res[i]["tree_size"]))
+        pick.add(max(idx, key=lambda i: res[i]["iterations"]))
+        pick.update(idx[:2])
+    for i in sorted(pick):
+        s, p, c = b.copy_tree(i)
+        check_tree_properties(qs[i], res[i], s, p, c, b.copy_path(i), n_edges=1000, seed=i)
+    b.close()
