@@ -265,6 +265,15 @@ KGMT_API kgmt_status kgmt_propagate_samples(const kgmt_config* cfg, const float*
                                    uint32_t n_obstacles, uint32_t n, float* d_x1, uint8_t* d_valid, int32_t* d_r1, int32_t* d_r2,
                                    void* stream);
 
+/* ---- failure-detection self-test (no counterpart in the reference) ---- */
+/* Runs the planning kernels' bounded look-back wait against a predecessor
+ * that never publishes, giving up after `polls` polls (1 .. 4194304).  The
+ * wait must time out: returns KGMT_ERR_TIMEOUT with the device error bits in
+ * *error_bits (bit 0: look-back timeout), as planning calls do when a bounded
+ * wait gives up; the context stays usable.  KGMT_ERR_INTERNAL if it did not
+ * time out.  Synchronous; a few kilobytes of device memory. */
+KGMT_API kgmt_status kgmt_selftest_bounded_wait(uint32_t polls, uint32_t* error_bits);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,6 +121,7 @@ SIGNATURES = {
     "kgmt_server_poll": (_i32, [_vp, _resp, _u32, _u32p]),
     "kgmt_propagate_samples": (_i32, [_cfgp, _vp, _vp, _vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     "kgmt_plan_noalloc": (_i32, [_cfgp, _vp, _vp, _vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, _resp, _vp]),
+    "kgmt_selftest_bounded_wait": (_i32, [_u32, _u32p]),
 }
 
 _lib = None

@@ -747,3 +747,32 @@ extern "C" kgmt_status kgmt_propagate_samples(const kgmt_config* cfg, const floa
       launch_propagate_samples(p, d_x0, d_uniforms, d_obstacles, n_obstacles, n, d_x1, d_valid, d_r1, d_r2, (cudaStream_t)stream),
       "k_propagate_samples");
 }
+
+extern "C" kgmt_status kgmt_selftest_bounded_wait(uint32_t polls, uint32_t* error_bits)
+{
+    RETURN_IF(!error_bits, KGMT_ERR_INVALID_ARG, "kgmt_selftest_bounded_wait: error_bits is NULL");
+    RETURN_IF(polls == 0 || polls > kSpinLimit, KGMT_ERR_INVALID_ARG, "kgmt_selftest_bounded_wait: polls outside 1 .. 4194304");
+    int dev_count = 0;
+    if(cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+        {
+            cudaGetLastError();
+            set_error("no CUDA device");
+            return KGMT_ERR_NO_DEVICE;
+        }
+    // two look-back words (tile 0 left empty) and the error word
+    void* d = nullptr;
+    CHECK_ST(cuda_status(cudaMalloc(&d, 3 * sizeof(unsigned long long)), "cudaMalloc"));
+    unsigned long long* tiles = (unsigned long long*)d;
+    uint32_t* err = (uint32_t*)(tiles + 2);
+    uint32_t h_err = 0;
+    cudaError_t e = cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+    if(e == cudaSuccess) e = launch_selftest_wait(tiles, err, polls, nullptr);
+    if(e == cudaSuccess) e = cudaMemcpy(&h_err, err, sizeof(h_err), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    CHECK_ST(cuda_status(e, "k_selftest_wait"));
+    *error_bits = h_err;
+    RETURN_IF(h_err & kErrLookbackTimeout, KGMT_ERR_TIMEOUT,
+              "kgmt_selftest_bounded_wait: a device-side wait gave up (error bits " + std::to_string(h_err) + ")");
+    set_error("kgmt_selftest_bounded_wait: the wait did not time out");
+    return KGMT_ERR_INTERNAL;
+}

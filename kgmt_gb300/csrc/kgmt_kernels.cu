@@ -49,7 +49,9 @@ constexpr unsigned long long kValMask = (1ull << 62) - 1;
 // Called by one full warp; lane i inspects predecessor lt-1-i, 32 at a time,
 // until the nearest inclusive prefix; every nearer predecessor must have
 // published at least its aggregate.  Returns the exclusive prefix on all lanes.
-__device__ unsigned long long lookback_warp(unsigned long long* tiles, int lt, uint32_t* error)
+// After `limit` polls without progress it records kErrLookbackTimeout in
+// *error and returns (the host reports KGMT_ERR_TIMEOUT).
+__device__ unsigned long long lookback_warp(unsigned long long* tiles, int lt, uint32_t* error, uint32_t limit = kSpinLimit)
 {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -67,7 +69,7 @@ __device__ unsigned long long lookback_warp(unsigned long long* tiles, int lt, u
             const unsigned upto = stop == 31 ? full : ((2u << stop) - 1u);
             if(not_ready & upto)
                 {
-                    if(++spins > kSpinLimit)
+                    if(++spins > limit)
                         {
                             if(lane == 0) atomicOr(error, kErrLookbackTimeout);
                             return prefix;
@@ -110,6 +112,20 @@ __device__ __forceinline__ void publish_and_lookback(unsigned long long* tiles, 
             st_volatile_u64(&tiles[lt], kStIncl | (prefix + agg));
             *s_prefix = prefix;
         }
+}
+
+// Failure-detection self-test: the look-back wait of tile 1 of a chain whose
+// tile 0 never publishes (a word nothing sets), with a short poll limit; it
+// must give up, record the timeout and return.  One warp.
+__global__ void k_selftest_wait(unsigned long long* tiles, uint32_t* error, uint32_t polls)
+{
+    lookback_warp(tiles, 1, error, polls);
+}
+
+cudaError_t launch_selftest_wait(unsigned long long* tiles, uint32_t* error, uint32_t polls, cudaStream_t s)
+{
+    k_selftest_wait<<<1, 32, 0, s>>>(tiles, error, polls);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -25,6 +25,8 @@ cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s);
 // src: rows of 2 * ws_dims floats (min corner, max corner)
 cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, int ws_dims, cudaStream_t s);
+// one warp waiting on a look-back word nothing sets, for at most `polls` polls
+cudaError_t launch_selftest_wait(unsigned long long* tiles, uint32_t* error, uint32_t polls, cudaStream_t s);
 cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, const float* u, const float* obs, uint32_t n_obs, uint32_t n,
                                      float* x1, uint8_t* valid, int32_t* r1, int32_t* r2, cudaStream_t s);
 int propagate_blocks_per_sm(int block, int models);

@@ -130,6 +130,8 @@ def test_no_device_fails_loudly(lib):
     with pytest.raises(_abi.KgmtError):
         from kgmt_gb300.planner import KGMT
         KGMT(double_integrator_single())
+    bits = C.c_uint32(0)
+    assert lib.kgmt_selftest_bounded_wait(1000, C.byref(bits)) == 6
 
 
 def test_null_arguments_rejected(lib):
@@ -139,3 +141,6 @@ def test_null_arguments_rejected(lib):
     assert lib.kgmt_server_poll(None, None, 0, None) == 1
     st = _abi.KgmtBatchStats()
     assert lib.kgmt_batch_get_stats(None, C.byref(st)) == 1
+    bits = C.c_uint32(0)
+    assert lib.kgmt_selftest_bounded_wait(1000, None) == 1
+    assert lib.kgmt_selftest_bounded_wait(0, C.byref(bits)) == 1

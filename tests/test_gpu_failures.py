@@ -1,0 +1,83 @@
+"""Failure detection without a GPU fault.
+
+- A bounded device-side wait that runs out: the planning kernels' look-back
+  wait, pointed at a predecessor that never publishes (a word nothing sets)
+  with a short poll limit, gives up and reports KGMT_ERR_TIMEOUT; the same
+  context then plans a query exactly as the oracle does.
+- Admission by device memory: a served query larger than the server's whole
+  memory budget is refused with KGMT_ERR_OOM, and the server keeps serving.
+Nothing here traps, faults or hangs the GPU."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from kgmt_gb300 import _abi
+from kgmt_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KGMT_ERR_OOM, KGMT_ERR_TIMEOUT = 2, 4
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return _abi.load()
+
+
+def plan_matches_oracle(q):
+    from kgmt_gb300.planner import KGMT
+    d_obs = torch.from_numpy(np.ascontiguousarray(W.boxes_for_plan(q), np.float32)).to("cuda:0")
+    p = KGMT(q.config)
+    res = p.plan(q.init, q.goal, d_obs, q.obstacles.shape[0])
+    samples, parents, _ = p.copy_tree()
+    p.close()
+    ref = O.plan(q)
+    for k in ("status", "iterations", "tree_size", "goal_index"):
+        assert res[k] == ref[k], (k, res[k], ref[k])
+    assert np.array_equal(parents, ref["parents"])
+    assert np.array_equal(samples.view(np.uint32), ref["samples"].view(np.uint32))
+
+
+@pytest.mark.parametrize("polls", [1, 1000, 100_000])
+def test_bounded_wait_times_out_and_the_context_survives(lib, polls):
+    bits = C.c_uint32(0)
+    rc = lib.kgmt_selftest_bounded_wait(polls, C.byref(bits))
+    assert rc == KGMT_ERR_TIMEOUT, lib.kgmt_last_error().decode()
+    assert bits.value & 1  # look-back timeout
+    assert "gave up" in lib.kgmt_last_error().decode()
+    plan_matches_oracle(W.double_integrator_query(seed=7))
+
+
+def test_selftest_rejects_unbounded_polls(lib):
+    bits = C.c_uint32(0)
+    assert lib.kgmt_selftest_bounded_wait(0, C.byref(bits)) == 1
+    assert lib.kgmt_selftest_bounded_wait((1 << 22) + 1, C.byref(bits)) == 1
+
+
+def test_server_refuses_a_query_over_its_memory_budget_and_keeps_serving(lib):
+    from kgmt_gb300.planner import Server
+    small = W.double_integrator_batch(3, seed=8, tree_capacity=5_000)
+    big = W.double_integrator_query(seed=2)
+    big.config = big.config.replace(tree_capacity=400_000)  # tens of MiB, over a 16 MiB budget
+    srv = Server(max_slots=2, memory_budget=16 << 20, iters_per_step=2)
+    with pytest.raises(_abi.KgmtError) as e:
+        srv.submit(big.config, big.init, big.goal, big.obstacles)
+    assert e.value.code == KGMT_ERR_OOM
+    tickets = {srv.submit(q.config, q.init, q.goal, q.obstacles): i for i, q in enumerate(small)}
+    got = {}
+    for _ in range(2000):
+        srv.step()
+        for r in srv.poll():
+            got[tickets[r["ticket"]]] = r
+        if len(got) == len(small):
+            break
+    refs = O.plan_batch(small)
+    for i, ref in enumerate(refs):
+        for k in ("status", "iterations", "tree_size", "goal_index"):
+            assert got[i][k] == ref[k], (i, k, got[i][k], ref[k])
