@@ -12,7 +12,9 @@ from pathlib import Path
 from .config import PlannerConfig
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "_lib" / "libkgmt.so"
+# KGMT_LIBRARY selects another build of the same ABI (e.g. the bounds-checked
+# _lib/libkgmt_checked.so)
+LIB_PATH = Path(os.environ["KGMT_LIBRARY"]) if os.environ.get("KGMT_LIBRARY") else PKG / "_lib" / "libkgmt.so"
 
 KGMT_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA", 6: "NO_DEVICE", 7: "NOT_READY",

@@ -24,6 +24,9 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 BUILD_DIR = PKG / "_build"
 LIB = OUT_DIR / "libkgmt.so"
+# the same sources with KGMT_CHECK_BOUNDS: the kernels test their scattered
+# indices and report a failure as KGMT_ERR_INTERNAL (a sanitizer stand-in)
+LIB_CHECKED = OUT_DIR / "libkgmt_checked.so"
 SOURCES = ["kgmt_kernels.cu", "kgmt_engine.cu", "kgmt_abi.cu", "kgmt_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -51,17 +54,21 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     BUILD_DIR.mkdir(exist_ok=True)
     OUT_DIR.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "kgmt.h"]
-    objs = []
+    objs, objs_checked = [], []
     jobs = []
     for src in SOURCES:
         s = CSRC / src
         o = BUILD_DIR / (s.stem + ".o")
+        oc = BUILD_DIR / (s.stem + "_checked.o")
         objs.append(o)
+        objs_checked.append(oc)
         if force or _stale(o, [s, *headers]):
             cmd = [nvcc(), *common_flags(), "-c", str(s), "-o", str(o)]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
+        if force or _stale(oc, [s, *headers]):
+            jobs.append([nvcc(), *common_flags(), "-DKGMT_CHECK_BOUNDS", "-c", str(s), "-o", str(oc)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             results = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
@@ -71,13 +78,14 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
                 print(r.stdout, r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+    for lib, os_ in ((LIB, objs), (LIB_CHECKED, objs_checked)):
+        if force or jobs or _stale(lib, os_):
+            tmp = lib.with_suffix(".so.tmp")
+            cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, os_), "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+            os.replace(tmp, lib)
     build_cli(force=force)
     return LIB
 

@@ -219,6 +219,7 @@ extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const 
     uint32_t err = 0;
     CHECK_ST(p->eng.read_states_and_error(0, 1, &p->state, &err));
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "kgmt_plan: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "kgmt_plan: an index check failed (bounds-checked build)");
     p->planned = true;
     return KGMT_OK;
 }
@@ -380,6 +381,7 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     CHECK_ST(b->eng.read_states_and_error(0, n, b->states.data(), &err));
     b->n_last = n;
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "batch: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "batch: an index check failed (bounds-checked build)");
     // counters of this call
     kgmt_batch_stats& s = b->stats;
     std::memset(&s, 0, sizeof(s));
@@ -705,6 +707,7 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
     uint32_t err = 0;
     CHECK_ST(s->eng.read_error(&err));
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "server: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "server: an index check failed (bounds-checked build)");
     if(n_running) *n_running = running;
     if(n_queued) *n_queued = (uint32_t)s->queue.size();
     return KGMT_OK;

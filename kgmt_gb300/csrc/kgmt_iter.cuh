@@ -76,6 +76,23 @@ __device__ __forceinline__ uint32_t atomic_add_release(uint32_t* p, uint32_t v)
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// KGMT_CHECK_BOUNDS builds (libkgmt_checked.so) test the kernels' scattered
+// indices against their buffers: a failed test records kErrBounds in
+// g_bounds_error and the access is skipped -- no trap, no fault -- and the
+// host reports KGMT_ERR_INTERNAL.  Other builds compile the tests away.
+// (Only kgmt_kernels.cu includes this header: the word is defined once.)
+#ifdef KGMT_CHECK_BOUNDS
+__device__ uint32_t g_bounds_error;
+__device__ __forceinline__ bool bound_ok(bool c)
+{
+    if(!c) atomicOr(&g_bounds_error, kErrBounds);
+    return c;
+}
+#define KGMT_BOUND(c) bound_ok(c)
+#else
+#define KGMT_BOUND(c) true
+#endif
+
 __device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p)
 {
     return *(const volatile unsigned long long*)p;
@@ -489,7 +506,9 @@ __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const P
 {
     constexpr int D = ModelDims<MODEL>::D;
     const uint32_t e = s / c.spe;
-    const uint32_t par = e < c.n_react ? p.rep_old[e] : p.rep_new[e - c.n_react];
+    uint32_t par = e < c.n_react ? (KGMT_BOUND(e < p.capacity) ? p.rep_old[e] : 0u)
+                                 : (KGMT_BOUND(e - c.n_react < p.capacity) ? p.rep_new[e - c.n_react] : 0u);
+    if(!KGMT_BOUND(par < p.capacity)) par = 0u;
     load_row_ro<D>(p.tree + (size_t)par * D, x0);
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
     constexpr bool four = ModelDims<MODEL>::NC == 4;
@@ -519,6 +538,7 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
             const CellIds cid = cell_ids(p, x1);
             r1 = cid.r1;
             bit = 1ull << cid.r2;
+            if(!KGMT_BOUND((uint32_t)r1 < p.regions && s < p.capacity)) live = ok = false;
             if(ok)
                 {
                     const uint64_t marks = p.marks[r1];
@@ -534,7 +554,7 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
                     store_row<D>(p.us + (size_t)s * D, x1);
                     p.up[s] = (int32_t)par;
                 }
-            p.ur1f[s] = (uint32_t)r1 | (acc ? 0x80000000u : 0u);
+            if(live) p.ur1f[s] = (uint32_t)r1 | (acc ? 0x80000000u : 0u);
         }
     // histogram updates (KGMT.cu:250-253): counter over all samples, valid
     // count and the fine-cell bit over the valid ones; one fire-and-forget L2

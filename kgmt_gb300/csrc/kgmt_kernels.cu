@@ -122,6 +122,18 @@ __global__ void k_selftest_wait(unsigned long long* tiles, uint32_t* error, uint
     lookback_warp(tiles, 1, error, polls);
 }
 
+uint32_t bounds_error_take()
+{
+#ifdef KGMT_CHECK_BOUNDS
+    uint32_t v = 0, z = 0;
+    if(cudaMemcpyFromSymbol(&v, g_bounds_error, sizeof(v)) != cudaSuccess) return kErrBounds;
+    cudaMemcpyToSymbol(g_bounds_error, &z, sizeof(z));
+    return v;
+#else
+    return 0u;
+#endif
+}
+
 cudaError_t launch_selftest_wait(unsigned long long* tiles, uint32_t* error, uint32_t polls, cudaStream_t s)
 {
     k_selftest_wait<<<1, 32, 0, s>>>(tiles, error, polls);
@@ -494,7 +506,11 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                     uint32_t pos = (uint32_t)s_prefix + excl;
 #pragma unroll
                     for(int j = 0; j < kOldPer; ++j)
-                        if(flags & (1u << j)) p.rep_old[pos++] = i0 + j;
+                        if(flags & (1u << j))
+                            {
+                                if(KGMT_BOUND(pos < p.capacity)) p.rep_old[pos] = i0 + j;
+                                ++pos;
+                            }
                 }
             else
                 {
@@ -560,6 +576,7 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                             if(!(acc_bits & (1u << j))) continue;
                             const uint32_t s = s0 + j;
                             const uint32_t idx = ia++;
+                            if(!KGMT_BOUND(idx < p.capacity && s < p.capacity)) continue;
                             // everything the sample needs is loaded before its
                             // first store (one round trip, not one per field)
                             const int32_t par = __ldg(p.up + s), r1 = rg[j];

@@ -25,6 +25,9 @@ cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_paths(const LaunchArgs& a, uint32_t n, cudaStream_t s);
 // src: rows of 2 * ws_dims floats (min corner, max corner)
 cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, int ws_dims, cudaStream_t s);
+// KGMT_CHECK_BOUNDS builds: the index-check error bits since the last call
+// (then cleared); always 0 in other builds
+uint32_t bounds_error_take();
 // one warp waiting on a look-back word nothing sets, for at most `polls` polls
 cudaError_t launch_selftest_wait(unsigned long long* tiles, uint32_t* error, uint32_t polls, cudaStream_t s);
 cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, const float* u, const float* obs, uint32_t n_obs, uint32_t n,

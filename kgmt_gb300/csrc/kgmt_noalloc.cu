@@ -169,6 +169,11 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
             set_error("kgmt_plan_noalloc: a device-side wait gave up (error bits " + std::to_string(err) + ")");
             return KGMT_ERR_TIMEOUT;
         }
+    if(bounds_error_take() != 0)
+        {
+            set_error("kgmt_plan_noalloc: an index check failed (bounds-checked build)");
+            return KGMT_ERR_INTERNAL;
+        }
     // outputs into the caller's buffers
     const uint32_t n = state.tree_size < max_nodes ? state.tree_size : max_nodes;
     const size_t D = params.sample_dim;

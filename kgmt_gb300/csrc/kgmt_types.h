@@ -88,6 +88,7 @@ inline uint32_t smem_boxes_for(uint32_t max_obs)
 // error bits in Sched::error
 constexpr uint32_t kErrLookbackTimeout = 1u;
 constexpr uint32_t kErrCopyTimeout = 2u;
+constexpr uint32_t kErrBounds = 4u;  // an index check of a KGMT_CHECK_BOUNDS build failed
 constexpr uint32_t kErrAppendMismatch = 4u;
 
 struct QueryParams {

@@ -81,3 +81,47 @@ def test_server_refuses_a_query_over_its_memory_budget_and_keeps_serving(lib):
     for i, ref in enumerate(refs):
         for k in ("status", "iterations", "tree_size", "goal_index"):
             assert got[i][k] == ref[k], (i, k, got[i][k], ref[k])
+
+
+CHECKED_SCRIPT = r'''
+import numpy as np, torch
+from kgmt_gb300 import workloads as W
+from kgmt_gb300.planner import KGMT, BatchPlanner
+from oracle import oracle as O
+qs = [W.double_integrator_query(seed=3), W.quadrotor_query(seed=1, tree_capacity=50_000, max_iterations=8),
+      W.dubins_query(seed=2), W.unicycle_query(seed=2)]
+for q in qs:
+    d_obs = torch.from_numpy(np.ascontiguousarray(W.boxes_for_plan(q), np.float32)).to("cuda:0")
+    p = KGMT(q.config)
+    res = p.plan(q.init, q.goal, d_obs, q.obstacles.shape[0])
+    s, par, c = p.copy_tree()
+    p.close()
+    ref = O.plan(q)
+    assert res["tree_size"] == ref["tree_size"] and np.array_equal(par, ref["parents"]), q.config.model
+    assert np.array_equal(s.view(np.uint32), ref["samples"].view(np.uint32)), q.config.model
+batch = W.double_integrator_batch(48, n_obstacles=50, seed=5, tree_capacity=20_000)
+inits, goals, obs, offs, cnts = W.pack_queries(batch)
+b = BatchPlanner(len(batch))
+res = b.plan([q.config for q in batch], inits, goals, obs, offs, cnts)
+for r, ref in zip(res, O.plan_batch(batch)):
+    assert (r["status"], r["iterations"], r["tree_size"]) == (ref["status"], ref["iterations"], ref["tree_size"])
+print("checked build ok")
+'''
+
+
+def test_bounds_checked_build_plans_like_the_oracle(lib):
+    """libkgmt_checked.so tests every scattered index of the kernels against
+    its buffer (a failed test is recorded and reported, the access skipped):
+    planning all four models and a batch through it gives the oracle's
+    results and no failed test (a failure would raise KGMT_ERR_INTERNAL)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    checked = root / "kgmt_gb300" / "_lib" / "libkgmt_checked.so"
+    assert checked.exists(), "build() makes the bounds-checked library"
+    env = dict(os.environ, KGMT_LIBRARY=str(checked), PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", CHECKED_SCRIPT], cwd=root, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "checked build ok" in r.stdout
