@@ -10,9 +10,21 @@
 #include <cmath>
 #include <cstring>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "kgmt_engine.h"
 
 namespace kgmt {
+
+// Names the host stages of the launch chain (admission, iteration units,
+// path readout) on a profiler's timeline; without a tool attached a range
+// costs a branch.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 thread_local std::string g_last_error;
 
@@ -505,6 +517,7 @@ kgmt_status Engine::schedule()
 
 kgmt_status Engine::admit(uint32_t first, uint32_t count, uint32_t n_active, const float* d_inits, const float* d_goals)
 {
+    NvtxRange r("kgmt admit");
     kgmt_status st = upload_params(first, count);
     if(st == KGMT_OK) st = set_active(n_active);
     if(st == KGMT_OK) st = init_slots(first, count, d_inits, d_goals);
@@ -593,6 +606,7 @@ kgmt_status Engine::build_graph()
 
 kgmt_status Engine::launch_unit()
 {
+    NvtxRange r(use_graph_ && !profile_ ? "kgmt iterations (graph replay)" : "kgmt iterations (direct launches)");
     if(use_graph_ && !profile_)
         {
             if(!graph_)
@@ -621,6 +635,7 @@ kgmt_status Engine::run_until_done(uint32_t max_iters)
     // running count the last schedule wrote (unit u-1's or a later one's) is
     // read from the mapped host word; nothing but the event record sits in
     // the stream between two graph replays.
+    NvtxRange r("kgmt run until done");
     const uint32_t G = iters_per_graph_;
     const uint32_t max_units = (max_iters + G - 1) / G + 2;
     volatile uint32_t* running = h_running_;
@@ -679,6 +694,7 @@ kgmt_status Engine::read_states_and_error(uint32_t first, uint32_t count, QueryS
 
 kgmt_status Engine::extract_paths(uint32_t n_active)
 {
+    NvtxRange r("kgmt paths");
     KGMT_CUDA(launch_paths(args(), n_active, stream_), "k_paths");
     launches_ += 1;
     return KGMT_OK;
