@@ -69,6 +69,36 @@ def test_cpp_wrapper_and_cli_compile(tmp_path, lib):
     assert (_abi.LIB_PATH.parent / "kgmt_plan").exists()
 
 
+def test_obstacle_csv_reader_throws_instead_of_exiting(tmp_path, lib):
+    """kgmt::read_obstacles_csv replaces readObstaclesFromCSV
+    (helper.cu:13-39), which calls exit(1): a missing file, a token that is
+    not a number and a partial box row each raise an exception the caller can
+    handle; well-formed files give 2W floats per box."""
+    (tmp_path / "ok3.csv").write_text("0.1, 0.2, 0.3, 0.4, 0.5, 0.6\n0.5,0.5,0.5,0.7,0.7,0.7\n")
+    (tmp_path / "ok2.csv").write_text("0.1,0.2,0.3,0.4\n")
+    (tmp_path / "text.csv").write_text("0.1,0.2,abc,0.4,0.5,0.6\n")
+    (tmp_path / "short.csv").write_text("0.1,0.2,0.3,0.4,0.5,0.6\n0.1,0.2,0.3\n")
+    src = tmp_path / "csv.cpp"
+    src.write_text(r"""#include "kgmt.hpp"
+#include <cstdio>
+static int kind(const char* path, int w) {
+    try { return (int)kgmt::read_obstacles_csv(path, w).size(); }
+    catch(const std::invalid_argument&) { return -2; }
+    catch(const std::runtime_error&) { return -1; }
+}
+int main(int, char** argv) {
+    std::string d = argv[1];
+    std::printf("%d %d %d %d %d\n", kind((d + "/ok3.csv").c_str(), 3), kind((d + "/ok2.csv").c_str(), 2),
+                kind((d + "/missing.csv").c_str(), 3), kind((d + "/text.csv").c_str(), 3), kind((d + "/short.csv").c_str(), 3));
+    return 0;
+}
+""")
+    subprocess.run(["g++", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(tmp_path / "csv"),
+                    f"-L{_abi.LIB_PATH.parent}", "-lkgmt", f"-Wl,-rpath,{_abi.LIB_PATH.parent}"], check=True)
+    r = subprocess.run([str(tmp_path / "csv"), str(tmp_path)], capture_output=True, text=True, check=True)
+    assert r.stdout.split() == ["12", "4", "-1", "-2", "-1"]
+
+
 def test_config_defaults_and_validation(lib):
     c = _abi.KgmtConfig()
     assert lib.kgmt_config_default(1, C.byref(c)) == 0
