@@ -73,6 +73,7 @@ typedef enum kgmt_status {
 #define KGMT_QUERY_SUCCESS 1    /* a node reached the goal ball            */
 #define KGMT_QUERY_ITER_LIMIT 2 /* max_iterations spent without the goal  */
 #define KGMT_QUERY_CAPACITY 3   /* tree full before the goal was reached   */
+#define KGMT_QUERY_CANCELLED 4  /* withdrawn by kgmt_server_cancel          */
 
 #define KGMT_MAX_SAMPLE_DIM 17
 #define KGMT_MAX_FINE_CELLS 64
@@ -235,6 +236,13 @@ KGMT_API kgmt_status kgmt_server_submit(kgmt_server* s, const kgmt_config* cfg, 
 KGMT_API kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uint32_t* n_queued);
 /* takes up to max finished results (FIFO by completion) */
 KGMT_API kgmt_status kgmt_server_poll(kgmt_server* s, kgmt_result* out, uint32_t max, uint32_t* n_out);
+/* Withdraws a submitted query between steps: a queued one is dropped, a
+ * resident one stops where its last step left it and frees its slot and
+ * memory.  Either way poll returns its result with status
+ * KGMT_QUERY_CANCELLED (a resident one with its iterations and tree size so
+ * far).  KGMT_ERR_NOT_READY when no queued or resident query has the ticket
+ * (unknown, or already finished). */
+KGMT_API kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket);
 
 /* ---- single query without any allocation ----
  * No counterpart in the reference (its planner allocates everything in its

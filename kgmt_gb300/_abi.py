@@ -121,6 +121,7 @@ SIGNATURES = {
     "kgmt_server_submit": (_i32, [_vp, _cfgp, _vp, _vp, _vp, _u32, C.POINTER(C.c_uint64)]),
     "kgmt_server_step": (_i32, [_vp, _u32p, _u32p]),
     "kgmt_server_poll": (_i32, [_vp, _resp, _u32, _u32p]),
+    "kgmt_server_cancel": (_i32, [_vp, C.c_uint64]),
     "kgmt_propagate_samples": (_i32, [_cfgp, _vp, _vp, _vp, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     "kgmt_plan_noalloc": (_i32, [_cfgp, _vp, _vp, _vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, _resp, _vp]),
     "kgmt_selftest_bounded_wait": (_i32, [_u32, _u32p]),

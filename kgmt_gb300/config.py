@@ -30,7 +30,8 @@ STATUS_RUNNING = 0
 STATUS_SUCCESS = 1
 STATUS_ITER_LIMIT = 2
 STATUS_CAPACITY = 3
-STATUS_NAMES = {0: "running", 1: "success", 2: "iteration-limit", 3: "capacity"}
+STATUS_CANCELLED = 4
+STATUS_NAMES = {0: "running", 1: "success", 2: "iteration-limit", 3: "capacity", 4: "cancelled"}
 
 MAX_SAMPLE_DIM = 17
 

@@ -581,6 +581,7 @@ struct kgmt_server {
     std::vector<QueryState> states;
     uint64_t next_ticket = 1;
     uint32_t running = 0;
+    bool resched = false;  // a resident query was cancelled: the next step recomputes the schedule
 };
 
 extern "C" kgmt_status kgmt_server_create(const kgmt_server_options* opt, void* stream, kgmt_server** out)
@@ -672,13 +673,14 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
             admitted = true;
             ++s->running;
         }
-    if(admitted)
+    if(admitted || s->resched)
         {
             int models = 0;
             for(size_t i = 0; i < s->slots.size(); ++i)
                 if(s->slots[i].used) models |= s->slots[i].model_bit;
             s->eng.set_models(models);
             CHECK_ST(s->eng.schedule());
+            s->resched = false;
         }
     // ---- iterations for every resident query ----
     if(s->running) CHECK_ST(s->eng.run_iterations(s->opt.iters_per_step));
@@ -711,6 +713,45 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
     if(n_running) *n_running = running;
     if(n_queued) *n_queued = (uint32_t)s->queue.size();
     return KGMT_OK;
+}
+
+extern "C" kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket)
+{
+    RETURN_IF(!s, KGMT_ERR_INVALID_ARG, "kgmt_server_cancel: NULL server");
+    const auto now = std::chrono::steady_clock::now();
+    for(auto it = s->queue.begin(); it != s->queue.end(); ++it)
+        if(it->ticket == ticket)
+            {
+                kgmt_result res;
+                std::memset(&res, 0, sizeof(res));
+                res.status = KGMT_QUERY_CANCELLED;
+                res.goal_index = -1;
+                res.ticket = ticket;
+                res.latency_ms = (float)(std::chrono::duration<double, std::milli>(now - it->submitted).count());
+                s->done.push_back(res);
+                s->queue.erase(it);
+                return KGMT_OK;
+            }
+    for(uint32_t i = 0; i < (uint32_t)s->slots.size(); ++i)
+        {
+            ResidentQuery& r = s->slots[i];
+            if(!r.used || r.ticket != ticket) continue;
+            // no kernel runs between steps: the status is final before the
+            // next step's schedule, which then gives the slot no tiles
+            CHECK_ST(s->eng.write_status(i, KGMT_QUERY_CANCELLED));
+            QueryState qs;
+            CHECK_ST(s->eng.read_states(i, 1, &qs));
+            kgmt_result res = to_result(qs, ticket);
+            res.latency_ms = (float)(std::chrono::duration<double, std::milli>(now - r.submitted).count());
+            s->done.push_back(res);
+            s->arena.release(r.offset);
+            r.used = false;
+            if(s->running) --s->running;
+            s->resched = true;
+            return KGMT_OK;
+        }
+    set_error("kgmt_server_cancel: no queued or running query has this ticket");
+    return KGMT_ERR_NOT_READY;
 }
 
 extern "C" kgmt_status kgmt_server_poll(kgmt_server* s, kgmt_result* out, uint32_t max, uint32_t* n_out)

@@ -673,6 +673,13 @@ kgmt_status Engine::read_states(uint32_t first, uint32_t count, QueryState* out)
     return KGMT_OK;
 }
 
+kgmt_status Engine::write_status(uint32_t slot, uint32_t status)
+{
+    KGMT_CUDA(cudaMemcpyAsync(&d_states_[slot].status, &status, sizeof(status), cudaMemcpyHostToDevice, stream_), "upload(status)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return KGMT_OK;
+}
+
 kgmt_status Engine::read_states_and_error(uint32_t first, uint32_t count, QueryState* out, uint32_t* err)
 {
     // both copies land in pinned staging, so they are queued together and

@@ -86,6 +86,8 @@ class Engine {
     // runs exactly `iters` iterations (served loop)
     kgmt_status run_iterations(uint32_t iters);
     kgmt_status read_states(uint32_t first, uint32_t count, QueryState* out);
+    // sets one slot's status on the device (between launches)
+    kgmt_status write_status(uint32_t slot, uint32_t status);
     // states and the error bits in one wait
     kgmt_status read_states_and_error(uint32_t first, uint32_t count, QueryState* out, uint32_t* err);
     kgmt_status extract_paths(uint32_t n_active);

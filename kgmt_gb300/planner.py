@@ -255,6 +255,11 @@ class Server:
         check(self._lib.kgmt_server_step(self._h, C.byref(r), C.byref(q)))
         return r.value, q.value
 
+    def cancel(self, ticket: int) -> None:
+        """Withdraws a queued or running query; poll() returns it with status
+        cancelled (KgmtError NOT_READY if it is unknown or already done)."""
+        check(self._lib.kgmt_server_cancel(self._h, ticket))
+
     def poll(self, max_results: int = 4096) -> list[dict]:
         out = (KgmtResult * max_results)()
         n = C.c_uint32()

@@ -169,6 +169,7 @@ def test_null_arguments_rejected(lib):
     assert lib.kgmt_plan(None, None, None, None, 0) == 1
     assert lib.kgmt_plan_batch(None, 0, None, None, None, None, None, None, None) == 1
     assert lib.kgmt_server_poll(None, None, 0, None) == 1
+    assert lib.kgmt_server_cancel(None, 1) == 1
     st = _abi.KgmtBatchStats()
     assert lib.kgmt_batch_get_stats(None, C.byref(st)) == 1
     bits = C.c_uint32(0)

@@ -125,3 +125,35 @@ def test_bounds_checked_build_plans_like_the_oracle(lib):
     r = subprocess.run([sys.executable, "-c", CHECKED_SCRIPT], cwd=root, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "checked build ok" in r.stdout
+
+
+def test_server_cancels_queued_and_running_queries(lib):
+    """A cancelled query leaves the server with status cancelled (a queued one
+    at iteration 0, a running one where its last step left it) and frees its
+    slot; the other queries' results are the oracle's, unaffected; an unknown
+    ticket is refused."""
+    from kgmt_gb300.planner import Server
+    qs = W.double_integrator_batch(5, seed=9, tree_capacity=20_000)
+    srv = Server(max_slots=2, memory_budget=1 << 28, iters_per_step=1)
+    tickets = [srv.submit(q.config, q.init, q.goal, q.obstacles) for q in qs]
+    srv.cancel(tickets[4])  # still queued
+    srv.step()              # admits the first two
+    srv.cancel(tickets[0])  # running
+    with pytest.raises(_abi.KgmtError) as e:
+        srv.cancel(10_000)
+    assert e.value.code == 7
+    got = {}
+    for _ in range(5000):
+        srv.step()
+        for r in srv.poll():
+            got[r["ticket"]] = r
+        if len(got) == len(qs):
+            break
+    assert got[tickets[4]]["status"] == 4 and got[tickets[4]]["iterations"] == 0
+    assert got[tickets[0]]["status"] == 4 and got[tickets[0]]["iterations"] >= 1
+    refs = O.plan_batch(qs[1:4])
+    for t, ref in zip(tickets[1:4], refs):
+        for k in ("status", "iterations", "tree_size", "goal_index"):
+            assert got[t][k] == ref[k], (t, k, got[t][k], ref[k])
+    with pytest.raises(_abi.KgmtError):
+        srv.cancel(tickets[1])  # finished
