@@ -7,7 +7,9 @@
 // (src/planners/KGMT.cu:84-95), which read sizes back from the device about
 // six times per iteration; here the schedule stays on the device.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include <nvtx3/nvToolsExt.h>
@@ -39,6 +41,21 @@ kgmt_status cuda_status(cudaError_t e, const char* what)
     return KGMT_ERR_CUDA;
 }
 
+// Every device allocation of the library goes through here.  With
+// KGMT_FAULT_ALLOC_AFTER=n in the environment (read once), each allocation
+// after the first n fails as out of memory without reaching the driver: a
+// host-side fault injector for the tests of the error paths.
+static cudaError_t device_alloc(void** p, size_t bytes)
+{
+    static const long limit = [] {
+        const char* e = std::getenv("KGMT_FAULT_ALLOC_AFTER");
+        return e ? std::atol(e) : -1L;
+    }();
+    static std::atomic<long> count{0};
+    if(limit >= 0 && count.fetch_add(1) >= limit) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
 #define KGMT_CUDA(call, what)                                 \
     do {                                                      \
         kgmt_status st_ = cuda_status((call), what);          \
@@ -66,7 +83,7 @@ kgmt_status DeviceArena::reserve(size_t bytes)
     cap_ = 0;
     free_.clear();
     bytes = (bytes + 4095) & ~size_t(4095);
-    KGMT_CUDA(cudaMalloc(&base_, bytes), "cudaMalloc(arena)");
+    KGMT_CUDA(device_alloc((void**)&base_, bytes), "cudaMalloc(arena)");
     cap_ = bytes;
     free_[0] = bytes;
     used_bytes_ = 0;
@@ -383,12 +400,12 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     iters_per_graph_ = iters_per_graph ? iters_per_graph : 4;
     use_graph_ = use_graph;
     h_params_.assign(slots, QueryParams{});
-    KGMT_CUDA(cudaMalloc(&d_params_, sizeof(QueryParams) * slots), "cudaMalloc(params)");
-    KGMT_CUDA(cudaMalloc(&d_states_, sizeof(QueryState) * slots), "cudaMalloc(states)");
-    KGMT_CUDA(cudaMalloc(&d_sched_, sizeof(Sched)), "cudaMalloc(sched)");
-    KGMT_CUDA(cudaMalloc(&d_tile_a_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
-    KGMT_CUDA(cudaMalloc(&d_tile_c_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
-    KGMT_CUDA(cudaMalloc(&d_tile_old_, sizeof(uint32_t) * slots), "cudaMalloc(tiles)");
+    KGMT_CUDA(device_alloc((void**)&d_params_, sizeof(QueryParams) * slots), "cudaMalloc(params)");
+    KGMT_CUDA(device_alloc((void**)&d_states_, sizeof(QueryState) * slots), "cudaMalloc(states)");
+    KGMT_CUDA(device_alloc((void**)&d_sched_, sizeof(Sched)), "cudaMalloc(sched)");
+    KGMT_CUDA(device_alloc((void**)&d_tile_a_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
+    KGMT_CUDA(device_alloc((void**)&d_tile_c_, sizeof(uint32_t) * (slots + 1)), "cudaMalloc(tiles)");
+    KGMT_CUDA(device_alloc((void**)&d_tile_old_, sizeof(uint32_t) * slots), "cudaMalloc(tiles)");
     // empty slots: zeroed params, status bytes 0xFF (kSlotEmpty), so no kernel
     // treats a slot as running before it is admitted
     KGMT_CUDA(cudaMemsetAsync(d_params_, 0, sizeof(QueryParams) * slots, stream_), "memset(params)");

@@ -157,3 +157,39 @@ def test_server_cancels_queued_and_running_queries(lib):
             assert got[t][k] == ref[k], (t, k, got[t][k], ref[k])
     with pytest.raises(_abi.KgmtError):
         srv.cancel(tickets[1])  # finished
+
+
+FAULT_SCRIPT = r'''
+from kgmt_gb300 import _abi, workloads as W
+from kgmt_gb300.planner import BatchPlanner
+from oracle import oracle as O
+qs = W.double_integrator_batch(4, seed=10, tree_capacity=5_000)
+inits, goals, obs, offs, cnts = W.pack_queries(qs)
+try:
+    b = BatchPlanner(len(qs))
+    res = b.plan([q.config for q in qs], inits, goals, obs, offs, cnts)
+    refs = O.plan_batch(qs)
+    same = all((r["status"], r["tree_size"]) == (f["status"], f["tree_size"]) for r, f in zip(res, refs))
+    b.close()
+    print("planned", same)
+except _abi.KgmtError as e:
+    print("error", e.code)
+'''
+
+
+@pytest.mark.parametrize("after,expect", [(0, "error 2"), (2, "error 2"), (5, "error 2"), (6, "error 2"), (1000, "planned True")])
+def test_injected_allocation_failure_is_an_error_not_a_crash(lib, after, expect):
+    """KGMT_FAULT_ALLOC_AFTER=n makes the library's (n+1)-th device
+    allocation fail as out of memory without reaching the driver (a host-side
+    injector): creating the batch engine (allocations 0-5) or growing its
+    arena while planning (6) then raises KGMT_ERR_OOM and the process exits
+    cleanly; with no failure in reach the batch plans as the oracle does."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, KGMT_FAULT_ALLOC_AFTER=str(after), PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", FAULT_SCRIPT], cwd=root, env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert r.stdout.strip().splitlines()[-1] == expect, r.stdout
