@@ -250,16 +250,24 @@ KGMT_API kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket);
  * device memory is owned by a fixed pool set up at start-up, real-time loops
  * that must never enter the allocator, hosts that forbid allocation after
  * initialisation.  The working memory lives in a static device array of
- * 32 MiB that every GPU loading this library holds until exit; queries that
- * need more (see kgmt_query_bytes) are rejected with KGMT_ERR_INVALID_ARG.
+ * KGMT_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU loading this library
+ * holds until exit; its first KGMT_NOALLOC_RESERVED_BYTES hold the planner's
+ * descriptors, so a query is accepted when
+ *     kgmt_query_bytes(cfg, n_obstacles) + KGMT_NOALLOC_RESERVED_BYTES <= KGMT_NOALLOC_SCRATCH_BYTES
+ * and rejected with KGMT_ERR_INVALID_ARG otherwise.
  * The caller passes the start / goal rows (host), the obstacles (device,
  * [n][6]) and device output buffers for up to max_nodes tree nodes
  * (samples [max_nodes][sample_dim], parents, costs) and max_path_rows path
- * rows (goal -> root); any output pointer may be NULL.  All calls on a device
- * share that one array and it keeps the last call's contents: calls that
- * overlap on the GPU (other threads, other streams) race and corrupt each
- * other.  The first call on a device looks up the array's address; make it
- * before any stream capture.  Blocks until done; stream may be NULL. */
+ * rows (goal -> root); any output pointer may be NULL; a host pointer where
+ * device memory is expected is rejected with KGMT_ERR_INVALID_ARG.  All calls
+ * on a device share that one array and it keeps the last call's contents:
+ * calls that overlap on the GPU (other threads, other streams) race and
+ * corrupt each other.  The first call on a device (and the first after its
+ * CUDA context is recreated) looks up the array's address; make it before
+ * any stream capture begins.  Every call waits for its stream before it
+ * returns; stream may be NULL. */
+#define KGMT_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define KGMT_NOALLOC_RESERVED_BYTES 4096u
 KGMT_API kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_initial, const float* h_goal, const float* d_obstacles,
                                        uint32_t n_obstacles, float* d_samples, int32_t* d_parents, float* d_costs, uint32_t max_nodes,
                                        float* d_path, uint32_t max_path_rows, kgmt_result* result, void* stream);

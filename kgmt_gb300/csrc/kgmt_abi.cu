@@ -150,17 +150,6 @@ extern "C" size_t kgmt_query_bytes(const kgmt_config* cfg, uint32_t n_obstacles)
     return layout_of(*cfg, n_obstacles, true).total;
 }
 
-static bool is_device_pointer(const void* p)
-{
-    cudaPointerAttributes a;
-    if(cudaPointerGetAttributes(&a, p) != cudaSuccess)
-        {
-            cudaGetLastError();
-            return false;
-        }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
 // ---------------------------------------------------------------------------
 // single planner
 // ---------------------------------------------------------------------------

@@ -56,6 +56,17 @@ static cudaError_t device_alloc(void** p, size_t bytes)
     return cudaMalloc(p, bytes);
 }
 
+bool is_device_pointer(const void* p)
+{
+    cudaPointerAttributes a;
+    if(cudaPointerGetAttributes(&a, p) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
 #define KGMT_CUDA(call, what)                                 \
     do {                                                      \
         kgmt_status st_ = cuda_status((call), what);          \

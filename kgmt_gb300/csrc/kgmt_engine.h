@@ -20,6 +20,9 @@ namespace kgmt {
 
 void set_error(const std::string& msg);
 kgmt_status cuda_status(cudaError_t e, const char* what);
+// device (or managed) memory the GPU may read and write; false for host
+// memory, unregistered pointers and NULL (allocates nothing)
+bool is_device_pointer(const void* p);
 
 // first-fit allocator over one device allocation
 class DeviceArena {

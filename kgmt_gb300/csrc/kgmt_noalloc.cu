@@ -11,52 +11,93 @@
 // the process exits.  The caller passes the obstacles and the output buffers.
 //
 // Rules of use:
-//  * queries whose working memory exceeds kNoAllocScratchBytes are rejected
-//    with KGMT_ERR_INVALID_ARG (kgmt_query_bytes() tells the size);
+//  * the first KGMT_NOALLOC_RESERVED_BYTES of the array hold the engine
+//    descriptors; a query whose working memory (kgmt_query_bytes()) exceeds
+//    the rest is rejected with KGMT_ERR_INVALID_ARG;
 //  * every call on a device shares the one array, and it keeps the contents
 //    of the last call: the entry point clears what must start at zero.  Calls
 //    that overlap on the GPU (two host threads, or two streams) race on the
 //    array and corrupt each other;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture.
-//  * no CUDA graph, event or stream is created; iterations are launched
-//    directly on the caller's stream.
+//  * the first call on a device, with that device current, looks up the
+//    array's device address (cudaGetSymbolAddress); the address is kept per
+//    CUDA context, so a context created anew (after cudaDeviceReset) is set
+//    up again by its first call.  Make that first call before any stream
+//    capture begins;
+//  * every call waits for its stream before it returns (the iteration count
+//    is read back between launches); no CUDA graph, event or stream is
+//    created.
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "kgmt_engine.h"
 
 namespace kgmt {
 
-constexpr size_t kNoAllocScratchBytes = 32ull << 20;  // 32 MiB per device
-constexpr int kNoAllocMaxDevices = 64;
+constexpr size_t kNoAllocScratchBytes = KGMT_NOALLOC_SCRATCH_BYTES;
+constexpr size_t kNoAllocReservedBytes = KGMT_NOALLOC_RESERVED_BYTES;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// host-side cache of the array's device address, one per device
-static unsigned char* g_scratch_addr[kNoAllocMaxDevices];
+// host-side cache of the array's device address, one entry per CUDA context
+// (keyed on the context's unique id, which a recreated context never reuses)
+static std::vector<std::pair<unsigned long long, unsigned char*>> g_scratch_addr;
 static std::mutex g_scratch_mu;
+
+// unique id of the calling thread's current context, through the driver entry
+// points the runtime hands out (no link against the driver library); false
+// when unavailable, and the address is then looked up on every call
+static bool current_context_id(unsigned long long* id)
+{
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+           q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)f;
+        f = nullptr;
+        if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+           q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)f;
+        cudaGetLastError();
+    });
+    if(!get_current || !get_id) return false;
+    CUcontext ctx = nullptr;
+    if(get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 static kgmt_status scratch_address(unsigned char** out)
 {
     int dev = 0;
     kgmt_status st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if(st != KGMT_OK) return st;
-    if(dev < 0 || dev >= kNoAllocMaxDevices)
-        {
-            set_error("kgmt_plan_noalloc: device index out of range");
-            return KGMT_ERR_INVALID_ARG;
-        }
+    // makes the device's primary context current on this thread (no allocation)
+    st = cuda_status(cudaSetDevice(dev), "cudaSetDevice");
+    if(st != KGMT_OK) return st;
+    unsigned long long id = 0;
+    const bool keyed = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if(g_scratch_addr[dev] == nullptr)
-        {
-            void* p = nullptr;
-            st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
-            if(st != KGMT_OK) return st;
-            g_scratch_addr[dev] = (unsigned char*)p;
-        }
-    *out = g_scratch_addr[dev];
+    if(keyed)
+        for(const auto& e : g_scratch_addr)
+            if(e.first == id)
+                {
+                    *out = e.second;
+                    return KGMT_OK;
+                }
+    void* p = nullptr;
+    st = cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+    if(st != KGMT_OK) return st;
+    if(keyed) g_scratch_addr.emplace_back(id, (unsigned char*)p);
+    *out = (unsigned char*)p;
     return KGMT_OK;
 }
 
@@ -94,18 +135,34 @@ extern "C" kgmt_status kgmt_plan_noalloc(const kgmt_config* cfg, const float* h_
             set_error("no CUDA device");
             return KGMT_ERR_NO_DEVICE;
         }
-    // working memory: engine descriptors, then the query chunk
+    // every pointer the kernels or the device-to-device copies touch must be
+    // device memory: a host pointer would be read or written by the GPU
+    // (cudaPointerGetAttributes allocates nothing)
+    const struct {
+        const void* p;
+        const char* what;
+    } dev_ptrs[] = {{n_obstacles ? d_obstacles : nullptr, "obstacles"}, {d_samples, "d_samples"}, {d_parents, "d_parents"},
+                    {d_costs, "d_costs"}, {d_path, "d_path"}};
+    for(const auto& d : dev_ptrs)
+        if(d.p && !is_device_pointer(d.p))
+            {
+                set_error(std::string("kgmt_plan_noalloc: ") + d.what + " must be a device pointer");
+                return KGMT_ERR_INVALID_ARG;
+            }
+    // working memory: engine descriptors in the reserved head, then the query chunk
     const size_t off_params = 0;
     const size_t off_state = round256(off_params + sizeof(QueryParams));
     const size_t off_sched = round256(off_state + sizeof(QueryState));
     const size_t off_tiles = round256(off_sched + sizeof(Sched));
-    const size_t off_chunk = round256(off_tiles + 5 * sizeof(uint32_t));
+    const size_t off_chunk = kNoAllocReservedBytes;
+    static_assert(((sizeof(QueryParams) + 255) / 256 + (sizeof(QueryState) + 255) / 256 + (sizeof(Sched) + 255) / 256 + 1) * 256 <=
+                    kNoAllocReservedBytes,
+                  "the engine descriptors fit the reserved head of the scratch array");
     const QueryLayout L = layout_of(*cfg, n_obstacles, true);
-    const size_t need = off_chunk + L.total;
-    if(need > kNoAllocScratchBytes)
+    if(L.total > kNoAllocScratchBytes - off_chunk)
         {
-            set_error("kgmt_plan_noalloc: the query needs " + std::to_string(need) + " bytes of working memory; the static scratch holds " +
-                      std::to_string(kNoAllocScratchBytes) + " (reduce tree_capacity, or use kgmt_plan)");
+            set_error("kgmt_plan_noalloc: the query needs " + std::to_string(L.total) + " bytes of working memory (kgmt_query_bytes); the static scratch holds " +
+                      std::to_string(kNoAllocScratchBytes - off_chunk) + " for a query (reduce tree_capacity, or use kgmt_plan)");
             return KGMT_ERR_INVALID_ARG;
         }
     unsigned char* base = nullptr;
