@@ -64,19 +64,27 @@ def test_di_fp64_oracle_tracks_reference(golden_dir):
     cfg = double_integrator_single().replace(di_rule=DI_RULE_REFERENCE)
     x1, valid = O.propagate_f64(cfg, g["x0"], g["u"], g["obstacles"])
     same = valid == g["valid"]
-    assert same.mean() > 0.995
+    # a verdict may differ only where the FP64 trajectory passes within 1e-6
+    # of a bound or a box face (none does in this fixture)
+    for i in np.flatnonzero(~same):
+        assert O.verdict_margin_f64(cfg, g["x0"][i], g["u"][i], g["obstacles"]) < 1e-6, i
     tol = REL_TOL * np.maximum(np.abs(x1), state_scales(cfg))
     assert np.all(np.abs(x1[same] - g["x1"][same]) <= tol[same])
 
 
 def test_quad_matches_reference_within_tolerance(golden_dir):
+    """Quadrotor (statePropagator.cu:246-370): the FP32 mirror and the FP64
+    restatement against the reference's propagateAndCheckQuadRungeKutta fed
+    the same uniforms.  Every verdict agrees except where the FP64 trajectory
+    passes within 1e-6 of a bound or a box face (none does here)."""
     g = np.load(golden_dir / "ref_quad.npz")
     cfg = quadrotor_large().replace(min_steps=1, max_steps=15)
     for fn in (O.propagate_f32, O.propagate_f64):
         out = fn(cfg, g["x0"], g["u"], g["obstacles"])
         x1, valid = out[0], out[1]
         same = valid == g["valid"]
-        assert same.mean() > 0.99, fn.__name__
+        for i in np.flatnonzero(~same):
+            assert O.verdict_margin_f64(cfg, g["x0"][i], g["u"][i], g["obstacles"]) < 1e-6, (fn.__name__, i)
         tol = REL_TOL * np.maximum(np.abs(g["x1"]), state_scales(cfg))
         bad = np.abs(x1[same] - g["x1"][same]) > tol[same]
         assert not bad.any(), (fn.__name__, np.argwhere(bad)[:5])
@@ -95,7 +103,6 @@ def test_new_models_match_reference_within_tolerance(golden_dir, fixture, cfg):
         same = valid == g["valid"]
         for i in np.flatnonzero(~same):
             assert O.verdict_margin_f64(cfg, g["x0"][i], g["u"][i], g["obstacles"]) < 1e-6, (fn.__name__, i)
-        assert same.mean() > 0.99, fn.__name__
         tol = REL_TOL * np.maximum(np.abs(g["x1"]), state_scales(cfg))
         bad = np.abs(x1[same] - g["x1"][same]) > tol[same]
         assert not bad.any(), (fn.__name__, np.argwhere(bad)[:5])
