@@ -122,6 +122,8 @@ typedef struct kgmt_result {
     float solve_ms;         /* admission -> completion, device clock           */
     float latency_ms;       /* server: submit -> retirement, host clock        */
     uint64_t ticket; /* server ticket / batch index */
+    float goal_cost; /* goal node's distance to the goal (h_costToGoal_), 0 if none */
+    uint32_t reserved;
 } kgmt_result;
 
 typedef struct kgmt_planner kgmt_planner;
@@ -156,6 +158,35 @@ KGMT_API kgmt_status kgmt_copy_path(kgmt_planner* p, float* h_rows, uint32_t max
 /* device pointers of the tree (d_treeSamples_, d_treeSamplesParentIdxs_,
  * d_treeSampleCosts_); valid until the next plan or destroy */
 KGMT_API kgmt_status kgmt_device_tree(kgmt_planner* p, const float** d_samples, const int32_t** d_parents, const float** d_costs);
+
+/* ---- traced plan: replaces KGMT::planBench (KGMT.cu:107-165) ----
+ * What one iteration left behind, as the reference's writeDeviceVectorsToCSV
+ * (KGMT.cu:405-488) dumps it after every iteration.  Host arrays owned by the
+ * planner, valid during the hook only. */
+typedef struct kgmt_iteration {
+    uint32_t itr;                /* h_itr_: the iteration just run (1-based)                      */
+    uint32_t tree_size;          /* h_treeSize_ after its append                                  */
+    uint32_t frontier_size;      /* h_frontierSize_: distinct frontier nodes it expanded          */
+    uint32_t expanded;           /* samples it propagated (the ExpandedNodes value)               */
+    uint32_t next_frontier_size; /* distinct nodes on the next frontier                           */
+    int32_t goal_index;          /* tree index of the goal node, -1 while none                    */
+    uint32_t path_len;           /* goal -> root rows in path once the goal is found, else 0      */
+    uint32_t capacity, sample_dim, regions;
+    const float* samples;   /* [capacity][sample_dim] d_treeSamples_; rows from tree_size on are 0  */
+    const int32_t* parents; /* [capacity] d_treeSamplesParentIdxs_; -1 from tree_size on           */
+    const int32_t* counter; /* [regions] samples per region so far (d_counterArray_)               */
+    const int32_t* valid;   /* [regions] valid samples per region (d_validCounterArray_)           */
+    const float* score;     /* [regions] region scores (d_vertexScoreArray_)                       */
+    const uint8_t* frontier; /* [capacity] 1: on the next frontier (d_frontier_)                   */
+    const uint32_t* repeat;  /* [capacity] its entries on the next frontier (d_activeFrontierRepeatCount_) */
+    const float* path;       /* [path_len][sample_dim] goal -> root (d_controlPathToGoal_)         */
+} kgmt_iteration;
+typedef void (*kgmt_iteration_hook)(const kgmt_iteration* it, void* user);
+/* kgmt_plan, one iteration per launch pair, calling hook(it, user) after
+ * every iteration with the state above; the same plan as kgmt_plan (a debug
+ * and analysis path: each iteration copies the tree back).  hook may be NULL. */
+KGMT_API kgmt_status kgmt_plan_traced(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                      uint32_t n_obstacles, kgmt_iteration_hook hook, void* user);
 
 /* ---- batched: many independent queries in one device-resident launch chain ---- */
 typedef struct kgmt_batch_options {

@@ -43,7 +43,7 @@ class KgmtConfig(C.Structure):
 class KgmtResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_uint32), ("tree_size", C.c_uint32), ("goal_index", C.c_int32),
                 ("path_len", C.c_uint32), ("samples_drawn", C.c_uint32), ("solve_ms", C.c_float), ("latency_ms", C.c_float),
-                ("ticket", C.c_uint64)]
+                ("ticket", C.c_uint64), ("goal_cost", C.c_float), ("reserved", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -70,6 +70,19 @@ class KgmtAutotuneResult(C.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class KgmtIteration(C.Structure):
+    """kgmt_iteration: what one iteration of a traced plan left behind."""
+    _fields_ = [("itr", C.c_uint32), ("tree_size", C.c_uint32), ("frontier_size", C.c_uint32), ("expanded", C.c_uint32),
+                ("next_frontier_size", C.c_uint32), ("goal_index", C.c_int32), ("path_len", C.c_uint32),
+                ("capacity", C.c_uint32), ("sample_dim", C.c_uint32), ("regions", C.c_uint32),
+                ("samples", C.POINTER(C.c_float)), ("parents", C.POINTER(C.c_int32)), ("counter", C.POINTER(C.c_int32)),
+                ("valid", C.POINTER(C.c_int32)), ("score", C.POINTER(C.c_float)), ("frontier", C.POINTER(C.c_uint8)),
+                ("repeat", C.POINTER(C.c_uint32)), ("path", C.POINTER(C.c_float))]
+
+
+ITERATION_HOOK = C.CFUNCTYPE(None, C.POINTER(KgmtIteration), C.c_void_p)
 
 
 class KgmtServerOptions(C.Structure):
@@ -107,6 +120,7 @@ SIGNATURES = {
     "kgmt_copy_tree": (_i32, [_vp, _vp, _vp, _vp, _u32]),
     "kgmt_copy_path": (_i32, [_vp, _vp, _u32, _u32p]),
     "kgmt_device_tree": (_i32, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
+    "kgmt_plan_traced": (_i32, [_vp, _vp, _vp, _vp, _u32, ITERATION_HOOK, _vp]),
     "kgmt_batch_create": (_i32, [C.POINTER(KgmtBatchOptions), _vp, C.POINTER(_vp)]),
     "kgmt_batch_destroy": (None, [_vp]),
     "kgmt_plan_batch": (_i32, [_vp, _u32, _cfgp, _vp, _vp, _vp, _vp, _vp, _resp]),

@@ -1,11 +1,13 @@
 // kgmt_plan -- command-line driver in the style of the reference's example
-// mains (examples/gpu/main.cu, executionTimeMain.cu): load an obstacle CSV,
-// copy it to the device, plan, report, and optionally export the tree and the
-// goal path as CSV files in the reference's layout (KGMT.cu:405-488).
+// mains (examples/gpu/main.cu, benchMain.cu, executionTimeMain.cu): load an
+// obstacle CSV, copy it to the device, plan, report, and optionally export
+// the tree and the goal path as CSV files in the reference's layout
+// (KGMT.cu:405-488).  --bench N runs planBench N times (bench runs 0..N-1),
+// as benchMain.cu does, writing the per-iteration files under ./Data.
 //
 //   kgmt_plan --obstacles scene.csv [--model di|quad] [--init x,y,z]
 //             [--goal x,y,z] [--seed N] [--capacity N] [--iterations N]
-//             [--repeat N] [--out DIR]
+//             [--repeat N] [--bench N] [--out DIR]
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -37,7 +39,7 @@ int main(int argc, char** argv)
     std::string obstacles, out;
     int model = KGMT_MODEL_DOUBLE_INTEGRATOR;
     std::vector<float> init = {0.05f, 0.05f, 0.05f}, goal = {0.95f, 0.95f, 0.95f};
-    long long seed = 1, capacity = -1, iterations = -1, repeat = 1;
+    long long seed = 1, capacity = -1, iterations = -1, repeat = 1, bench = 0;
     for(int i = 1; i < argc; ++i)
         {
             std::string a = argv[i];
@@ -57,11 +59,12 @@ int main(int argc, char** argv)
             else if(a == "--capacity" && v) capacity = std::atoll(v), ++i;
             else if(a == "--iterations" && v) iterations = std::atoll(v), ++i;
             else if(a == "--repeat" && v) repeat = std::atoll(v), ++i;
+            else if(a == "--bench" && v) bench = std::atoll(v), ++i;
             else if(a == "--out" && v) out = v, ++i;
             else
                 {
                     std::fprintf(stderr, "usage: %s --obstacles scene.csv [--model di|quad|dubins|unicycle] [--init x,y,z] [--goal x,y,z] "
-                                         "[--seed N] [--capacity N] [--iterations N] [--repeat N] [--out DIR]\n", argv[0]);
+                                         "[--seed N] [--capacity N] [--iterations N] [--repeat N] [--bench N] [--out DIR]\n", argv[0]);
                     return 2;
                 }
         }
@@ -93,8 +96,17 @@ int main(int argc, char** argv)
                     planner.plan(h_init.data(), h_goal.data(), d_obs, n);
                     double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
                     const kgmt_result& res = planner.result();
-                    std::printf("KGMT execution time: %.6f seconds. Iterations: %u. Tree Size: %u. Status: %d. Goal: %d. Path: %u\n",
-                                ms * 1e-3, planner.h_itr_, planner.h_treeSize_, res.status, res.goal_index, res.path_len);
+                    std::printf("KGMT execution time: %.6f seconds. Iterations: %u. Tree Size: %u. Status: %d. Goal: %d. Path: %u. "
+                                "Cost to goal: %.9g\n",
+                                ms * 1e-3, planner.h_itr_, planner.h_treeSize_, res.status, res.goal_index, res.path_len,
+                                (double)planner.h_costToGoal_);
+                }
+            // benchMain.cu:27-32: planBench once per bench run
+            for(long long b = 0; b < bench; ++b)
+                {
+                    planner.planBench(h_init.data(), h_goal.data(), d_obs, n, (int)b);
+                    std::printf("KGMT bench %lld: Iterations: %u. Tree Size: %u. Goal: %d\n", b, planner.h_itr_, planner.h_treeSize_,
+                                planner.h_pathToGoal_);
                 }
             if(!out.empty())
                 {
@@ -104,8 +116,7 @@ int main(int argc, char** argv)
                     kgmt::write_csv(out + "/samples.csv", samples.data(), planner.h_treeSize_, D);
                     kgmt::write_csv(out + "/parents.csv", parents.data(), planner.h_treeSize_, 1);
                     kgmt::write_csv(out + "/costs.csv", costs.data(), planner.h_treeSize_, 1);
-                    kgmt::write_csv(out + "/controlPathToGoal.csv", planner.h_controlPathToGoal_.data(),
-                                    planner.h_controlPathToGoal_.size() / D, D);
+                    kgmt::write_csv(out + "/controlPathToGoal.csv", planner.h_controlPathToGoal_, planner.h_pathLength_, D);
                 }
             if(d_obs) cudaFree(d_obs);
         }

@@ -1,5 +1,6 @@
 // kgmt_abi.cu -- the C ABI (include/kgmt.h): single planner, batch, server
 // and the function-level propagation entry.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -183,32 +184,137 @@ extern "C" kgmt_status kgmt_create(const kgmt_config* cfg, void* stream, kgmt_pl
 
 extern "C" void kgmt_destroy(kgmt_planner* p) { delete p; }
 
-extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles,
-                                 uint32_t n_obstacles)
+// set-up shared by kgmt_plan and kgmt_plan_traced: the query's buffers in
+// the planner's arena, its boxes staged, the query admitted and the first
+// schedule computed (KGMT.cu:48-81)
+static kgmt_status plan_setup(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles, uint32_t n_obstacles,
+                              const char* who)
 {
-    RETURN_IF(!p || !h_initial || !h_goal, KGMT_ERR_INVALID_ARG, "kgmt_plan: NULL argument");
-    RETURN_IF(n_obstacles > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, "kgmt_plan: obstacles pointer is NULL");
+    RETURN_IF(!p || !h_initial || !h_goal, KGMT_ERR_INVALID_ARG, std::string(who) + ": NULL argument");
+    RETURN_IF(n_obstacles > 0 && !d_obstacles, KGMT_ERR_INVALID_ARG, std::string(who) + ": obstacles pointer is NULL");
     RETURN_IF(n_obstacles > 0 && !is_device_pointer(d_obstacles), KGMT_ERR_INVALID_ARG,
-              "kgmt_plan: obstacles must be a device pointer (as in KGMT::plan)");
+              std::string(who) + ": obstacles must be a device pointer (as in KGMT::plan)");
     p->planned = false;
     const QueryLayout L = layout_of(p->cfg, n_obstacles, true);
     p->arena.reset();
     CHECK_ST(p->arena.reserve(L.total));
     size_t off = 0;
-    RETURN_IF(!p->arena.alloc(L.total, &off), KGMT_ERR_OOM, "kgmt_plan: arena allocation failed");
+    RETURN_IF(!p->arena.alloc(L.total, &off), KGMT_ERR_OOM, std::string(who) + ": arena allocation failed");
     p->params = make_params(p->cfg, h_initial, h_goal, p->arena.base() + off, L, nullptr, n_obstacles);
     CHECK_ST(cuda_status(launch_stage_obstacles(d_obstacles, p->params.obstacles, n_obstacles, (int)ws_dims_of(p->cfg.model), p->eng.stream()),
                          "stage obstacles"));
     p->eng.host_params(0) = p->params;
     p->eng.set_models(Engine::model_bit(p->cfg.model));
     p->eng.set_max_obstacles(n_obstacles);
-    CHECK_ST(p->eng.admit(0, 1, 1));
+    return p->eng.admit(0, 1, 1);
+}
+
+extern "C" kgmt_status kgmt_plan(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                 uint32_t n_obstacles)
+{
+    CHECK_ST(plan_setup(p, h_initial, h_goal, d_obstacles, n_obstacles, "kgmt_plan"));
     CHECK_ST(p->eng.run_until_done(p->cfg.max_iterations));
     CHECK_ST(p->eng.extract_paths(1));
     uint32_t err = 0;
     CHECK_ST(p->eng.read_states_and_error(0, 1, &p->state, &err));
     RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "kgmt_plan: a device-side wait gave up (error bits " + std::to_string(err) + ")");
     RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "kgmt_plan: an index check failed (bounds-checked build)");
+    p->planned = true;
+    return KGMT_OK;
+}
+
+// device -> pageable host copy on the planner's stream, waited for
+static kgmt_status copy_back(cudaStream_t s, void* dst, const void* src, size_t bytes, const char* what)
+{
+    if(bytes == 0) return KGMT_OK;
+    CHECK_ST(cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), what));
+    return cuda_status(cudaStreamSynchronize(s), what);
+}
+
+// KGMT::planBench (KGMT.cu:107-165): the same plan one iteration at a time,
+// with the state writeDeviceVectorsToCSV (KGMT.cu:405-488) dumps handed to
+// the hook after each iteration.  Only the rows appended by the iteration are
+// copied back; the next frontier's flags and repeat counts are rebuilt on the
+// host from the two frontier lists.
+extern "C" kgmt_status kgmt_plan_traced(kgmt_planner* p, const float* h_initial, const float* h_goal, const float* d_obstacles,
+                                        uint32_t n_obstacles, kgmt_iteration_hook hook, void* user)
+{
+    CHECK_ST(plan_setup(p, h_initial, h_goal, d_obstacles, n_obstacles, "kgmt_plan_traced"));
+    const QueryParams& prm = p->params;
+    const uint32_t T = prm.capacity, D = prm.sample_dim, R1 = prm.regions;
+    const cudaStream_t s = p->eng.stream();
+    std::vector<float> samples((size_t)T * D, 0.0f), score(R1), path(((size_t)prm.max_iterations + 2) * D, 0.0f);
+    std::vector<int32_t> parents(T, -1), counter(R1), valid(R1);
+    std::vector<uint8_t> frontier(T, 0);
+    std::vector<uint32_t> repeat(T, 0), list(T);
+    QueryState before, after;
+    uint32_t err = 0;
+    CHECK_ST(p->eng.read_states_and_error(0, 1, &before, &err));
+    CHECK_ST(copy_back(s, samples.data(), prm.tree, (size_t)D * 4, "copy root"));
+    parents[0] = -1;
+    uint32_t new_nodes = 1;  // nodes the previous iteration appended (the root before the first)
+    for(uint32_t k = 0; k < prm.max_iterations + 2 && before.status == KGMT_QUERY_RUNNING; ++k)
+        {
+            CHECK_ST(p->eng.run_iterations(1));
+            CHECK_ST(p->eng.read_states_and_error(0, 1, &after, &err));
+            RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "kgmt_plan_traced: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+            if(after.status != KGMT_QUERY_RUNNING)
+                {
+                    CHECK_ST(p->eng.extract_paths(1));
+                    CHECK_ST(p->eng.read_states_and_error(0, 1, &after, &err));
+                }
+            // rows appended by this iteration (earlier rows never change)
+            const uint32_t t0 = before.tree_size, t1 = after.tree_size < T ? after.tree_size : T;
+            if(t1 > t0)
+                {
+                    CHECK_ST(copy_back(s, samples.data() + (size_t)t0 * D, prm.tree + (size_t)t0 * D, (size_t)(t1 - t0) * D * 4, "copy rows"));
+                    CHECK_ST(copy_back(s, parents.data() + t0, prm.parent + t0, (size_t)(t1 - t0) * 4, "copy parents"));
+                }
+            CHECK_ST(copy_back(s, counter.data(), prm.counter, (size_t)R1 * 4, "copy counters"));
+            CHECK_ST(copy_back(s, valid.data(), prm.valid, (size_t)R1 * 4, "copy valid counts"));
+            CHECK_ST(copy_back(s, score.data(), prm.score, (size_t)R1 * 4, "copy scores"));
+            // the next frontier: re-activated nodes once each, then new nodes
+            // with their repeat counts
+            std::fill(frontier.begin(), frontier.end(), 0);
+            std::fill(repeat.begin(), repeat.end(), 0u);
+            uint32_t distinct = 0;
+            const uint32_t n_old = after.n_react < T ? after.n_react : T, n_new = after.w_new < T ? after.w_new : T;
+            CHECK_ST(copy_back(s, list.data(), prm.rep_old, (size_t)n_old * 4, "copy frontier"));
+            for(uint32_t i = 0; i < n_old; ++i)
+                if(list[i] < T) frontier[list[i]] = 1, repeat[list[i]] += 1, ++distinct;
+            CHECK_ST(copy_back(s, list.data(), prm.rep_new, (size_t)n_new * 4, "copy frontier"));
+            for(uint32_t i = 0; i < n_new; ++i)
+                if(list[i] < T)
+                    {
+                        if(!frontier[list[i]]) ++distinct;
+                        frontier[list[i]] = 1, repeat[list[i]] += 1;
+                    }
+            const uint32_t rows = after.path_len < prm.max_iterations + 2 ? after.path_len : prm.max_iterations + 2;
+            if(after.status == KGMT_QUERY_SUCCESS && rows)
+                CHECK_ST(copy_back(s, path.data(), prm.path, (size_t)rows * D * 4, "copy path"));
+            if(hook)
+                {
+                    kgmt_iteration it;
+                    std::memset(&it, 0, sizeof(it));
+                    it.itr = before.itr;
+                    it.tree_size = after.tree_size;
+                    it.frontier_size = before.n_react + new_nodes;
+                    it.expanded = before.n_samples;
+                    it.next_frontier_size = distinct;
+                    it.goal_index = after.status == KGMT_QUERY_SUCCESS ? after.goal_index : -1;
+                    it.path_len = after.status == KGMT_QUERY_SUCCESS ? rows : 0;
+                    it.capacity = T, it.sample_dim = D, it.regions = R1;
+                    it.samples = samples.data(), it.parents = parents.data();
+                    it.counter = counter.data(), it.valid = valid.data(), it.score = score.data();
+                    it.frontier = frontier.data(), it.repeat = repeat.data(), it.path = path.data();
+                    hook(&it, user);
+                }
+            new_nodes = after.tree_size - before.tree_size;
+            before = after;
+        }
+    RETURN_IF(before.status == KGMT_QUERY_RUNNING, KGMT_ERR_INTERNAL, "kgmt_plan_traced: the query did not stop within its iteration budget");
+    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "kgmt_plan_traced: an index check failed (bounds-checked build)");
+    p->state = before;
     p->planned = true;
     return KGMT_OK;
 }

@@ -351,6 +351,7 @@ kgmt_result to_result(const QueryState& s, uint64_t ticket)
     r.samples_drawn = s.samples_drawn;
     r.solve_ms = s.t_end > s.t_start ? (float)((double)(s.t_end - s.t_start) * 1e-6) : 0.0f;
     r.ticket = ticket;
+    r.goal_cost = s.status == KGMT_QUERY_SUCCESS && s.path_len > 0 ? s.goal_cost : 0.0f;
     return r;
 }
 

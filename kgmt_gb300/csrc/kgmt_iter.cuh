@@ -798,6 +798,10 @@ __device__ inline void finalize_query(const QueryParams& p, QueryState& st, Sche
     else if(tree >= cap) status = KGMT_QUERY_CAPACITY;
     st.tree_size = tree;
     st.samples_drawn = drawn + ns;
+    // the next frontier's list lengths (kept for a finished query too: the
+    // traced plan reports its last frontier)
+    st.n_react = react_total;
+    st.w_new = w_total;
     // per-iteration accumulators start from zero next iteration
     st.tiles_done = 0;
     st.prop_done = 0;
@@ -812,8 +816,6 @@ __device__ inline void finalize_query(const QueryParams& p, QueryState& st, Sche
             st.t_end = globaltimer();
             return;
         }
-    st.n_react = react_total;
-    st.w_new = w_total;
     st.itr = itr + 1;
     st.n_next = 0;
     uint32_t spe, n_samples;

@@ -659,6 +659,7 @@ __global__ void k_paths(const QueryParams* __restrict__ P, QueryState* S, uint32
             ++len;
             i = p.parent[i];
         }
+    st.goal_cost = p.cost[st.goal_index];
     st.path_len = len;
 }
 

@@ -89,7 +89,7 @@ inline uint32_t smem_boxes_for(uint32_t max_obs)
 constexpr uint32_t kErrLookbackTimeout = 1u;
 constexpr uint32_t kErrCopyTimeout = 2u;
 constexpr uint32_t kErrBounds = 4u;  // an index check of a KGMT_CHECK_BOUNDS build failed
-constexpr uint32_t kErrAppendMismatch = 4u;
+constexpr uint32_t kErrAppendMismatch = 8u;  // appended samples != accepted samples
 
 struct QueryParams {
     int32_t model;
@@ -169,6 +169,7 @@ struct QueryState {
     float score_total;
     uint32_t samples_drawn;
     uint32_t path_len;
+    float goal_cost;      // the goal node's cost (set with the path)
     unsigned long long t_start;  // %globaltimer at admission (ns)
     unsigned long long t_end;
     unsigned long long steps;    // RK4 steps executed over all samples

@@ -73,6 +73,51 @@ class KGMT:
         self.h_controlPathToGoal_ = self.copy_path()
         return self.result
 
+    def plan_traced(self, h_initial, h_goal, d_obstacles_ptr, h_obstaclesCount: int, hook=None) -> list[dict] | dict:
+        """``KGMT::planBench`` (src/planners/KGMT.cu:107-165) without the
+        files: the same plan one iteration at a time.  ``hook(it)`` gets a
+        dict per iteration (sizes and numpy copies of the tree rows, region
+        tables and next frontier); without a hook the dicts are returned."""
+        D = self.config.sample_dim
+        init = np.zeros(D, np.float32)
+        goal = np.zeros(D, np.float32)
+        a = _f32(h_initial).ravel()
+        g = _f32(h_goal).ravel()
+        init[: min(D, a.size)] = a[:D]
+        goal[: min(D, g.size)] = g[:D]
+        out = []
+
+        def on_iteration(it_p, _user):
+            it = it_p.contents
+            T, Dd, R = it.capacity, it.sample_dim, it.regions
+            arr = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy()  # noqa: E731
+            d = {f: getattr(it, f) for f in ("itr", "tree_size", "frontier_size", "expanded", "next_frontier_size",
+                                             "goal_index", "path_len")}
+            d["samples"] = arr(it.samples, T * Dd).reshape(T, Dd)
+            d["parents"] = arr(it.parents, T)
+            d["counter"] = arr(it.counter, R)
+            d["valid"] = arr(it.valid, R)
+            d["score"] = arr(it.score, R)
+            d["frontier"] = arr(it.frontier, T)
+            d["repeat"] = arr(it.repeat, T)
+            d["path"] = arr(it.path, it.path_len * Dd).reshape(it.path_len, Dd) if it.path_len else np.zeros((0, Dd), np.float32)
+            if hook is None:
+                out.append(d)
+            else:
+                hook(d)
+
+        cb = _abi.ITERATION_HOOK(on_iteration)
+        check(self._lib.kgmt_plan_traced(self._h, init.ctypes.data, goal.ctypes.data, ptr(d_obstacles_ptr), int(h_obstaclesCount),
+                                         cb, None))
+        r = KgmtResult()
+        check(self._lib.kgmt_get_result(self._h, C.byref(r)))
+        self.result = r.as_dict()
+        self.h_treeSize_ = r.tree_size
+        self.h_itr_ = r.iterations
+        self.h_pathToGoal_ = r.goal_index if r.goal_index > 0 else 0
+        self.h_controlPathToGoal_ = self.copy_path()
+        return out if hook is None else self.result
+
     def copy_tree(self):
         n = self.h_treeSize_
         D = self.config.sample_dim

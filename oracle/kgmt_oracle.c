@@ -942,6 +942,12 @@ float ko_f_accept(uint32_t itr, float eps, uint32_t tree_size, uint32_t n_next, 
 int ko_plan(const ko_config* c, const float* init, const float* goal, const float* obstacles, uint32_t n_obs, ko_result* res,
             float* samples, int32_t* parents, float* costs, float* path, ko_iter_trace* trace)
 {
+    return ko_plan_hooked(c, init, goal, obstacles, n_obs, res, samples, parents, costs, path, trace, NULL, NULL);
+}
+
+int ko_plan_hooked(const ko_config* c, const float* init, const float* goal, const float* obstacles, uint32_t n_obs, ko_result* res,
+                   float* samples, int32_t* parents, float* costs, float* path, ko_iter_trace* trace, ko_iter_hook hook, void* user)
+{
     const int D = ko_sample_dim(c->model);
     const uint32_t T = c->tree_capacity;
     const uint32_t S = c->samples_per_node;
@@ -983,6 +989,7 @@ int ko_plan(const ko_config* c, const float* init, const float* goal, const floa
     int status = KO_STATUS_RUNNING;
     int32_t goal_idx = -1;
     uint32_t itr = 0, drawn = 0;
+    uint32_t new_nodes = 1; /* nodes appended by the last iteration (the root before the first) */
 
     while(status == KO_STATUS_RUNNING)
         {
@@ -1071,6 +1078,28 @@ int ko_plan(const ko_config* c, const float* init, const float* goal, const floa
                     tr->f_accept = fa;
                     tr->score_total = total;
                 }
+            if(hook)
+                {
+                    /* h_frontierSize_ (KGMT.cu:171-172): the distinct nodes this
+                     * iteration expanded, re-activated ones and the last
+                     * iteration's new ones */
+                    ko_iter_view v;
+                    v.itr = itr;
+                    v.tree_size = tree_size + n_next;
+                    v.frontier_size = n_react + new_nodes;
+                    v.expanded = N;
+                    v.n_react = nr;
+                    v.n_rep_new = w < T ? w : T;
+                    v.goal_index = goal_idx;
+                    v.regions = R1;
+                    v.rep_old = rep_old;
+                    v.rep_new = rep_new;
+                    v.counter = counter;
+                    v.valid = validc;
+                    v.score = score;
+                    hook(&v, user);
+                }
+            new_nodes = n_next;
             tree_size += n_next;
             n_react = nr;
             w_new = w;

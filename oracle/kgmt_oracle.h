@@ -143,11 +143,35 @@ void ko_score_update(const ko_config* c, const int32_t* counter, const int32_t* 
                      float* score, float* total_out);
 float ko_f_accept(uint32_t itr, float eps, uint32_t tree_size, uint32_t n_next, uint32_t capacity);
 
+/* What one iteration leaves behind, for the per-iteration dump of the
+ * reference's planBench (KGMT.cu:107-165, writeDeviceVectorsToCSV 405-488):
+ * sizes, the cumulative region tables after the iteration's scores, and the
+ * next frontier as the two index lists (re-activated nodes, then new nodes
+ * each repeated 15 or 1 times).  Pointers are valid during the hook only. */
+typedef struct ko_iter_view {
+    uint32_t itr;
+    uint32_t tree_size;     /* after the iteration's append */
+    uint32_t frontier_size; /* distinct frontier nodes the iteration expanded */
+    uint32_t expanded;      /* samples it propagated */
+    uint32_t n_react, n_rep_new;
+    int32_t goal_index;     /* -1 while none */
+    uint32_t regions;
+    const uint32_t* rep_old;
+    const uint32_t* rep_new;
+    const int32_t* counter;
+    const int32_t* valid;
+    const float* score;
+} ko_iter_view;
+typedef void (*ko_iter_hook)(const ko_iter_view* view, void* user);
+
 /* Whole plan (FP32 mirror).  samples: capacity*sample_dim, parents/costs:
  * capacity; path: (max_iterations+2)*sample_dim rows goal->root.  trace may be
  * NULL or hold max_iterations entries. */
 int ko_plan(const ko_config* c, const float* init, const float* goal, const float* obstacles, uint32_t n_obs, ko_result* res,
             float* samples, int32_t* parents, float* costs, float* path, ko_iter_trace* trace);
+/* ko_plan calling hook(view, user) after every iteration */
+int ko_plan_hooked(const ko_config* c, const float* init, const float* goal, const float* obstacles, uint32_t n_obs, ko_result* res,
+                   float* samples, int32_t* parents, float* costs, float* path, ko_iter_trace* trace, ko_iter_hook hook, void* user);
 
 /* n independent queries; OpenMP over queries with `threads` threads (0 = all).
  * Only results (no trees) are returned.  obstacles concatenated as rows of 6

@@ -35,6 +35,16 @@ class KoResult(C.Structure):
                 ("path_len", C.c_uint32), ("samples_drawn", C.c_uint32)]
 
 
+class KoIterView(C.Structure):
+    _fields_ = [("itr", C.c_uint32), ("tree_size", C.c_uint32), ("frontier_size", C.c_uint32), ("expanded", C.c_uint32),
+                ("n_react", C.c_uint32), ("n_rep_new", C.c_uint32), ("goal_index", C.c_int32), ("regions", C.c_uint32),
+                ("rep_old", C.POINTER(C.c_uint32)), ("rep_new", C.POINTER(C.c_uint32)), ("counter", C.POINTER(C.c_int32)),
+                ("valid", C.POINTER(C.c_int32)), ("score", C.POINTER(C.c_float))]
+
+
+KO_ITER_HOOK = C.CFUNCTYPE(None, C.POINTER(KoIterView), C.c_void_p)
+
+
 class KoTrace(C.Structure):
     _fields_ = [("itr", C.c_uint32), ("tree_size_before", C.c_uint32), ("n_samples", C.c_uint32),
                 ("samples_per_entry", C.c_uint32), ("n_next", C.c_uint32), ("n_react", C.c_uint32),
@@ -92,6 +102,8 @@ def load():
         lib.ko_f_accept.restype = f
         lib.ko_f_accept.argtypes = [C.c_uint32, f, C.c_uint32, C.c_uint32, C.c_uint32]
         lib.ko_plan.argtypes = [cfgp, fp, fp, fp, C.c_uint32, C.POINTER(KoResult), fp, i32p, fp, fp, C.POINTER(KoTrace)]
+        lib.ko_plan_hooked.argtypes = [cfgp, fp, fp, fp, C.c_uint32, C.POINTER(KoResult), fp, i32p, fp, fp, C.POINTER(KoTrace),
+                                       KO_ITER_HOOK, C.c_void_p]
         lib.ko_plan_batch.argtypes = [C.c_uint32, cfgp, fp, fp, fp, u32p, u32p, C.POINTER(KoResult), C.c_int]
         _lib = lib
     return _lib
@@ -217,8 +229,12 @@ def f_accept(itr, eps, tree_size, n_next, capacity) -> float:
     return float(load().ko_f_accept(itr, eps, tree_size, n_next, capacity))
 
 
-def plan(query, trace: bool = False):
-    """Run one query; returns dict with result fields, tree and path."""
+def plan(query, trace: bool = False, tables: bool = False):
+    """Run one query; returns dict with result fields, tree and path.  With
+    ``tables`` also ``out["tables"]``: per iteration the sizes, the region
+    counters, valid counts and scores after it, and the next frontier as
+    per-node flags and repeat counts (what the reference's planBench dumps,
+    KGMT.cu:405-488)."""
     cfg = query.config
     k = to_ko(cfg)
     D = cfg.sample_dim
@@ -232,9 +248,27 @@ def plan(query, trace: bool = False):
     init = _f32(query.init)
     goal = _f32(query.goal)
     obs = boxes(cfg, query.obstacles)
-    rc = load().ko_plan(C.byref(k), _ptr(init, C.c_float), _ptr(goal, C.c_float), _ptr(obs, C.c_float), obs.shape[0],
-                        C.byref(res), _ptr(samples, C.c_float), _ptr(parents, C.c_int32), _ptr(costs, C.c_float),
-                        _ptr(path, C.c_float), tr)
+    snaps = []
+
+    def on_iteration(v_p, _user):
+        v = v_p.contents
+        arr = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0)  # noqa: E731
+        frontier = np.zeros(T, np.uint8)
+        repeat = np.zeros(T, np.uint32)
+        old = arr(v.rep_old, v.n_react).astype(np.int64)
+        new = arr(v.rep_new, v.n_rep_new).astype(np.int64)
+        frontier[old] = 1
+        frontier[new] = 1
+        np.add.at(repeat, old, 1)
+        np.add.at(repeat, new, 1)
+        snaps.append(dict(itr=v.itr, tree_size=v.tree_size, frontier_size=v.frontier_size, expanded=v.expanded,
+                          goal_index=v.goal_index, next_frontier_size=int(frontier.sum()), counter=arr(v.counter, v.regions),
+                          valid=arr(v.valid, v.regions), score=arr(v.score, v.regions), frontier=frontier, repeat=repeat))
+
+    hook = KO_ITER_HOOK(on_iteration) if tables else KO_ITER_HOOK()
+    rc = load().ko_plan_hooked(C.byref(k), _ptr(init, C.c_float), _ptr(goal, C.c_float), _ptr(obs, C.c_float), obs.shape[0],
+                               C.byref(res), _ptr(samples, C.c_float), _ptr(parents, C.c_int32), _ptr(costs, C.c_float),
+                               _ptr(path, C.c_float), tr, hook, None)
     if rc != 0:
         raise RuntimeError(f"ko_plan failed: {rc}")
     out = dict(status=res.status, iterations=res.iterations, tree_size=res.tree_size, goal_index=res.goal_index,
@@ -244,6 +278,8 @@ def plan(query, trace: bool = False):
     out["parents"] = parents[:n]
     out["costs"] = costs[:n]
     out["path"] = path[: res.path_len]
+    if tables:
+        out["tables"] = snaps
     if trace:
         out["trace"] = [dict((f, getattr(tr[i], f)) for f, _ in KoTrace._fields_) for i in range(res.iterations)]
     return out
