@@ -1,8 +1,8 @@
 """Generate the golden vectors in tests/golden/ from the reference's own code.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run with the path of a checkout of the reference's sources:
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    python tests/golden/make_golden.py --ref /path/to/reference
 
 It compiles the reference's propagation, collision and region functions for
 the host (oracle/ref/Makefile -> oracle/_ref/*.so), feeds them seeded inputs
@@ -229,7 +229,7 @@ def philox_kat():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="checkout of the reference's sources (read only)")
     args = ap.parse_args()
     libs = load_ref(args.ref)
     assert libs["di"].ref_model() == 1 and libs["quad"].ref_model() == 3
