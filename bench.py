@@ -42,6 +42,19 @@ WORKLOAD = (f"batched homogeneous: {N_QUERIES} double-integrator queries per GPU
             f"(edges U[0.05,0.15]), own start/goal, T={CAPACITY} nodes, S=4 samples/node, <=200 iterations, "
             f"8^3/2^3 region grid")
 L2_FLUSH_BYTES = 256 << 20
+L2_NOTE = ("trees, frontiers and samples of a step are ~1.4 GB, larger than L2; the GPU arm also flushes L2 "
+           "(256 MiB write) between timed steps")
+# configs 4 and 5 measured beside the headline: the mixed batch and a served
+# Poisson stream drawn from it
+N_MIXED = 1024
+MIXED_PLAIN_SAMPLE = 32
+SERVED_RATES = (1000.0, 4000.0)
+SERVED_QUERIES = 2000
+
+
+def config_of(world: int) -> dict:
+    """The same `config` in both arms: what is planned per step."""
+    return {"workload": WORKLOAD, "queries_per_step": N_QUERIES * world, "l2": L2_NOTE}
 
 
 def dist_env():
@@ -134,12 +147,43 @@ class ClockSampler:
                 "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
 
 
-# DRAM bytes (read + write) per k_propagate launch on this workload, from one
-# ncu capture of a planning step (dram__bytes_read.sum + dram__bytes_write.sum
-# summed over its 132 propagate launches, --cache-control none --clock-control
-# none): 551 MB read + 592 MB written.  The live algorithmic bytes per launch
-# are reported beside it.
-PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH = (551.45e6 + 592.36e6) / 132
+# DRAM traffic of k_propagate comes from an ncu capture of the current kernel
+# sources on a small case of this workload, summarised under profiles/ with
+# the hash of the sources it was taken on; a summary of other sources is
+# stale and gives no traffic figure (null).
+TRAFFIC_PROFILE = ROOT / "profiles" / "k_propagate_dram_batched_di64.md"
+KERNEL_SOURCES = ["kgmt_kernels.cu", "kgmt_iter.cuh", "kgmt_device.cuh", "kgmt_types.h"]
+
+
+def kernel_source_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        h.update((ROOT / "kgmt_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def propagate_traffic(samples_per_launch: float) -> dict:
+    """DRAM bytes per k_propagate launch of this workload: the captured
+    bytes per propagated sample times this run's samples per launch (traffic
+    grows with the samples: each reads its parent row and writes its region
+    word, the accepted ones their rows)."""
+    import re
+    if not TRAFFIC_PROFILE.exists():
+        return {"traffic": None, "traffic_note": f"{TRAFFIC_PROFILE.name} missing"}
+    text = TRAFFIC_PROFILE.read_text()
+    sha = re.search(r"kernel_source_hash:\s*(\w+)", text)
+    per = re.search(r"dram_bytes_per_sample:\s*([0-9.eE+]+)", text)
+    if not sha or not per:
+        return {"traffic": None, "traffic_note": f"{TRAFFIC_PROFILE.name} has no figures"}
+    if sha.group(1) != kernel_source_hash():
+        return {"traffic": None, "traffic_note": f"{TRAFFIC_PROFILE.name} was captured on other kernel sources"}
+    b = float(per.group(1))
+    return {"traffic": b * samples_per_launch, "traffic_bytes_per_sample": b,
+            "traffic_note": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per sample from {TRAFFIC_PROFILE.name} "
+                            f"(a small case of this workload, sources {sha.group(1)}), times this run's samples per launch"}
+
+
 # algorithmic bytes of the double-integrator propagate: per sample the
 # frontier index and the parent's row (10 floats) read and the region-and-
 # accept word written; per sample that joins the tree also its row and parent
@@ -230,8 +274,8 @@ def run_reference(args) -> None:
     line = {
         "impl": "reference", "metric": "planning queries/sec", "value": value, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox scenes)",
-        "config": {"workload": WORKLOAD, "parallelism": f"OpenMP over queries, {threads} threads"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox scenes, no dataset)",
+        "config": config_of(1), "parallelism": f"OpenMP over queries, {threads} threads",
         "success_rate": succ / (N_QUERIES * args.steps),
         "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"the full {N_QUERIES}-query batch per step; CPU restatement of the reference planner "
@@ -357,14 +401,22 @@ def run_ours(args) -> None:
         plain_succ = sum(r["status"] == 1 for r in plain_res) / n_plain
         cpu = cpu_baseline(queries)
         peaks = measured_peaks()
+        # ---- configs 4 and 5: the mixed batch, and a served stream from it ----
+        from kgmt_gb300 import measure as M
+        mixed_qs = W.mixed_batch(N_MIXED, seed=1)
+        mixed = M.mixed_line(mixed_qs, reps=3, plain_sample=MIXED_PLAIN_SAMPLE)
+        served = []
+        for rate in SERVED_RATES:
+            sv = M.served_line(mixed_qs, rate, SERVED_QUERIES)
+            sv["served_over_plain"] = sv["queries_per_s"] / mixed["plain"]["queries_per_s"]
+            served.append(sv)
         total_kernel_ms = st["ms_propagate"] + st["ms_score"] + st["ms_append"]
         line = {
             "metric": "planning queries/sec", "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox scenes, no dataset)",
-            "config": {"workload": WORKLOAD, "queries_per_step": N_QUERIES * ws, "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": "query-sharded (one 256-query shard per GPU)", "propagate_block": 256,
-                       "iters_per_graph": 4},
+            "config": config_of(ws), "parallelism": "query-sharded (one 256-query shard per GPU)",
+            "settings": {"propagate_block": 256, "iters_per_graph": 4},
             "p50_solve_ms": float(np.percentile(solve, 50)), "p99_solve_ms": float(np.percentile(solve, 99)),
             "success_rate": success,
             "plain": {"value": plain_qps, "unit": "queries/s", "queries": n_plain, "success_rate": plain_succ,
@@ -375,8 +427,8 @@ def run_ours(args) -> None:
                     "d2h_bytes_per_step": d2h},
             "roofline": {"kernel": "k_propagate", "bound": "fp32", "achieved": achieved * 1e-12, "peak": fp32_peak * 1e-12,
                          "unit": "T FP32 lane-ops/s", "frac": achieved / fp32_peak,
-                         "traffic": PROPAGATE_TRAFFIC_BYTES_PER_LAUNCH,
-                         "traffic_unit": "DRAM bytes per launch (ncu capture of this workload)",
+                         **propagate_traffic(st["samples"] / max(1, st["launches_propagate"])),
+                         "traffic_unit": "DRAM bytes per launch",
                          "algorithmic_bytes_per_launch": (st["samples"] * PROPAGATE_BYTES_PER_SAMPLE
                                                           + sum(r["tree_size"] - 1 for r in last) * PROPAGATE_BYTES_PER_ACCEPTED)
                          / max(1, st["launches_propagate"]),
@@ -386,6 +438,10 @@ def run_ours(args) -> None:
             "kernel_ms": {"propagate": st["ms_propagate"], "score": st["ms_score"], "append": st["ms_append"],
                           "iterations": st["iterations_launched"], "samples": st["samples"],
                           "steps": st["steps_executed"], "obstacle_tests": st["obstacle_tests"]},
+            "mixed": mixed,
+            "served": {"plain_queries_per_s": mixed["plain"]["queries_per_s"],
+                       "plain_note": "the plain form serves one query per launch chain: its rate is the mixed batch's plain rate",
+                       "streams": served},
             "hbm_peak_gbs": peaks.get("hbm_gbs"),
             "cpu_baseline": cpu,
             "clocks": clk,

@@ -129,66 +129,77 @@ def m_batch(args):
             "iterations_launched": st["iterations_launched"], "kernel_launches": st["kernel_launches"]}
 
 
-def m_mixed(args):
-    qs = W.mixed_batch(args.n_mixed, seed=1)
-    walls, res, st = _batched(qs, args.reps)
+def mixed_line(qs, reps: int, plain_sample: int) -> dict:
+    """The heterogeneous batch planned in one launch chain (best of `reps`
+    host-clocked runs after a warm-up), and the plain form -- one query per
+    launch chain -- on `plain_sample` of the same queries spread over the
+    batch, with their results compared."""
+    walls, res, st = _batched(qs, reps)
     wall = min(walls)
     solve = [r["solve_ms"] for r in res]
-    # plain form on a sample of the same queries: same results, its own speed
-    idx = list(range(0, len(qs), max(1, len(qs) // args.plain_sample)))[: args.plain_sample]
+    idx = list(range(0, len(qs), max(1, len(qs) // plain_sample)))[:plain_sample]
     ptimes, pres = plain_run([qs[i] for i in idx])
     same = all(pres[k]["tree_size"] == res[i]["tree_size"] and pres[k]["goal_index"] == res[i]["goal_index"]
-               for k, i in enumerate(idx))
+               and pres[k]["iterations"] == res[i]["iterations"] for k, i in enumerate(idx))
     by_model = {}
     for q, r in zip(qs, res):
         m = "quad" if q.config.model == 3 else "di"
         by_model.setdefault(m, []).append(r["status"] == 1)
+    plain_qps = len(ptimes) / (sum(ptimes) * 1e-3)
     return {"workload": f"batched heterogeneous {len(qs)} queries (half DI, half quad; 5..1000 boxes; grids 8^3..32^3; "
                         f"T 10k..500k)", "queries": len(qs), "queries_per_s": len(qs) / wall, "batch_ms": wall * 1e3,
             "p50_solve_ms": _pct(solve, 50), "p99_solve_ms": _pct(solve, 99),
             "success_rate": float(np.mean([r["status"] == 1 for r in res])),
             "success_by_model": {k: float(np.mean(v)) for k, v in by_model.items()},
             "iterations_launched": st["iterations_launched"],
-            "plain": {"queries": len(idx), "queries_per_s": len(ptimes) / (sum(ptimes) * 1e-3),
-                      "p50_solve_ms": _pct(ptimes, 50), "p99_solve_ms": _pct(ptimes, 99),
+            "plain": {"queries": len(idx), "sample": f"every {max(1, len(qs) // plain_sample)}-th query of the batch",
+                      "queries_per_s": plain_qps, "p50_solve_ms": _pct(ptimes, 50), "p99_solve_ms": _pct(ptimes, 99),
+                      "success_rate": float(np.mean([r["status"] == 1 for r in pres])),
                       "results_identical_to_batched": same},
-            "batched_over_plain": (len(qs) / wall) / (len(ptimes) / (sum(ptimes) * 1e-3))}
+            "batched_over_plain": (len(qs) / wall) / plain_qps}
+
+
+def served_line(pool, rate: float, n: int, slots: int = 1024, budget_gb: float = 150.0, iters_per_step: int = 2,
+                seed: int | None = None) -> dict:
+    """A Poisson stream of n queries drawn in order from `pool`, offered at
+    `rate` queries/s to a server (continuous batching, admission by device
+    memory); latency is submit -> result, host clock."""
+    arrivals = W.poisson_arrivals(n, rate, seed=int(rate) if seed is None else seed)
+    srv = Server(max_slots=slots, memory_budget=int(budget_gb * (1 << 30)), iters_per_step=iters_per_step)
+    t0 = time.perf_counter()
+    nxt, done, lat, solve, succ = 0, 0, [], [], []
+    steps = 0
+    while done < n:
+        now = time.perf_counter() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            q = pool[nxt % len(pool)]
+            srv.submit(q.config, q.init, q.goal, q.obstacles)
+            nxt += 1
+        running, queued = srv.step()
+        steps += 1
+        for r in srv.poll():
+            done += 1
+            lat.append(r["latency_ms"])
+            solve.append(r["solve_ms"])
+            succ.append(r["status"] == 1)
+        if running == 0 and queued == 0 and nxt < n:
+            time.sleep(max(0.0, min(0.001, arrivals[nxt] - (time.perf_counter() - t0))))
+    wall = time.perf_counter() - t0
+    srv.close()
+    return {"workload": f"served Poisson stream at {rate:.0f} queries/s from the mixed set", "offered_qps": rate,
+            "queries": n, "queries_per_s": n / wall, "p50_latency_ms": _pct(lat, 50), "p99_latency_ms": _pct(lat, 99),
+            "p50_solve_ms": _pct(solve, 50), "p99_solve_ms": _pct(solve, 99),
+            "success_rate": float(np.mean(succ)), "server_steps": steps, "slots": slots, "memory_budget_gb": budget_gb}
+
+
+def m_mixed(args):
+    return mixed_line(W.mixed_batch(args.n_mixed, seed=1), args.reps, args.plain_sample)
 
 
 def m_served(args):
     pool = W.mixed_batch(args.n_mixed, seed=2)
-    rates = [float(r) for r in args.rates.split(",")]
-    out = []
-    for rate in rates:
-        n = args.n_served
-        arrivals = W.poisson_arrivals(n, rate, seed=int(rate))
-        srv = Server(max_slots=args.slots, memory_budget=int(args.budget_gb * (1 << 30)), iters_per_step=args.iters_per_step)
-        t0 = time.perf_counter()
-        nxt, done, lat, solve, succ = 0, 0, [], [], []
-        steps = 0
-        while done < n:
-            now = time.perf_counter() - t0
-            while nxt < n and arrivals[nxt] <= now:
-                q = pool[nxt % len(pool)]
-                srv.submit(q.config, q.init, q.goal, q.obstacles)
-                nxt += 1
-            running, queued = srv.step()
-            steps += 1
-            for r in srv.poll():
-                done += 1
-                lat.append(r["latency_ms"])
-                solve.append(r["solve_ms"])
-                succ.append(r["status"] == 1)
-            if running == 0 and queued == 0 and nxt < n:
-                time.sleep(max(0.0, min(0.001, arrivals[nxt] - (time.perf_counter() - t0))))
-        wall = time.perf_counter() - t0
-        srv.close()
-        out.append({"workload": f"served Poisson stream at {rate:.0f} queries/s from the mixed set", "offered_qps": rate,
-                    "queries": n, "queries_per_s": n / wall, "p50_latency_ms": _pct(lat, 50), "p99_latency_ms": _pct(lat, 99),
-                    "p50_solve_ms": _pct(solve, 50), "p99_solve_ms": _pct(solve, 99),
-                    "success_rate": float(np.mean(succ)), "server_steps": steps, "slots": args.slots,
-                    "memory_budget_gb": args.budget_gb})
-    return out
+    return [served_line(pool, float(r), args.n_served, args.slots, args.budget_gb, args.iters_per_step)
+            for r in args.rates.split(",")]
 
 
 def main(argv=None) -> int:
