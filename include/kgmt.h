@@ -205,8 +205,12 @@ typedef struct kgmt_batch_stats {
     uint64_t samples;             /* samples propagated                            */
     uint64_t fp32_ops;            /* algorithmic FP32 operations of k_propagate    */
     uint32_t iterations_launched; /* iterations launched (incl. the no-op tail)    */
-    uint32_t launches_propagate, launches_score, launches_append;
-    float ms_propagate, ms_score, ms_append; /* summed CUDA-event time (profile_kernels) */
+    uint32_t launches_propagate, launches_tail, launches_append;
+    float ms_propagate, ms_tail, ms_append; /* summed CUDA-event time (profile_kernels) */
+    uint32_t iterations_tail;     /* iterations run by the persistent tail launches */
+    uint32_t reserved;
+    uint64_t fp32_ops_tail;       /* the part of fp32_ops the tail launches did      */
+    uint64_t samples_tail;        /* the part of samples the tail launches propagated */
 } kgmt_batch_stats;
 
 KGMT_API kgmt_status kgmt_batch_create(const kgmt_batch_options* opt, void* stream, kgmt_batch** out);

@@ -57,8 +57,10 @@ class KgmtBatchOptions(C.Structure):
 class KgmtBatchStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("steps_executed", C.c_uint64), ("obstacle_tests", C.c_uint64),
                 ("samples", C.c_uint64), ("fp32_ops", C.c_uint64), ("iterations_launched", C.c_uint32),
-                ("launches_propagate", C.c_uint32), ("launches_score", C.c_uint32), ("launches_append", C.c_uint32),
-                ("ms_propagate", C.c_float), ("ms_score", C.c_float), ("ms_append", C.c_float)]
+                ("launches_propagate", C.c_uint32), ("launches_tail", C.c_uint32), ("launches_append", C.c_uint32),
+                ("ms_propagate", C.c_float), ("ms_tail", C.c_float), ("ms_append", C.c_float),
+                ("iterations_tail", C.c_uint32), ("reserved", C.c_uint32), ("fp32_ops_tail", C.c_uint64),
+                ("samples_tail", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

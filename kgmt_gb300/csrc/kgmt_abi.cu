@@ -495,8 +495,14 @@ static kgmt_status batch_run(kgmt_batch* b, uint32_t n, const kgmt_config* cfgs,
     float ms[3];
     uint32_t cnt[3];
     CHECK_ST(b->eng.kernel_times(ms, cnt));
-    s.ms_propagate = ms[0], s.ms_score = ms[1], s.ms_append = ms[2];
-    s.launches_propagate = cnt[0], s.launches_score = cnt[1], s.launches_append = cnt[2];
+    s.ms_propagate = ms[0], s.ms_tail = ms[1], s.ms_append = ms[2];
+    s.launches_propagate = cnt[0], s.launches_tail = cnt[1], s.launches_append = cnt[2];
+    uint32_t tail_iters = 0;
+    uint64_t tail_ops = 0, tail_samples = 0;
+    CHECK_ST(b->eng.tail_counters(&tail_iters, &tail_ops, &tail_samples));
+    s.iterations_tail = tail_iters;
+    s.fp32_ops_tail = tail_ops;
+    s.samples_tail = tail_samples;
     if(results)
         for(uint32_t i = 0; i < n; ++i) results[i] = to_result(b->states[i], i);
     return KGMT_OK;

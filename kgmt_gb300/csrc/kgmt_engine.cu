@@ -383,6 +383,7 @@ Engine::~Engine()
     cudaFree(d_tile_a_);
     cudaFree(d_tile_c_);
     cudaFree(d_tile_old_);
+    cudaFree(d_tail_);
     if(own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -425,8 +426,16 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     KGMT_CUDA(cudaMemsetAsync(d_tile_a_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_c_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_old_, 0, sizeof(uint32_t) * slots, stream_), "memset");
-    // the running count, written by the device into mapped pinned memory
-    KGMT_CUDA(cudaHostAlloc((void**)&h_running_, sizeof(uint32_t) * 2, cudaHostAllocMapped), "cudaHostAlloc(mapped)");
+    KGMT_CUDA(device_alloc((void**)&d_tail_, tail_scratch_bytes()), "cudaMalloc(tail)");
+    KGMT_CUDA(cudaMemsetAsync(d_tail_, 0, tail_scratch_bytes(), stream_), "memset(tail)");
+    {
+        const char* e = std::getenv("KGMT_TAIL");
+        tail_on_ = !(e && e[0] == '0');
+    }
+    // the running count and the tail launch's report, written by the device
+    // into mapped pinned memory
+    KGMT_CUDA(cudaHostAlloc((void**)&h_running_, sizeof(uint32_t) * 4, cudaHostAllocMapped), "cudaHostAlloc(mapped)");
+    std::memset(h_running_, 0, sizeof(uint32_t) * 4);
     KGMT_CUDA(cudaHostGetDevicePointer((void**)&d_running_, h_running_, 0), "cudaHostGetDevicePointer");
     KGMT_CUDA(cudaMallocHost((void**)&h_stage_states_, sizeof(QueryState) * slots), "cudaMallocHost(states)");
     for(auto& e : ev_) KGMT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
@@ -446,6 +455,14 @@ kgmt_status Engine::set_prop_block(uint32_t block)
     KGMT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     for(int m : {1, 2, 4, 8, 15}) grid_a_[m] = sms * propagate_blocks_per_sm((int)block, m);
     grid_c_ = sms * append_blocks_per_sm();
+    // the tail launch: one block per SM (all blocks resident for its grid-wide
+    // barriers), iterations up to two samples per thread
+    for(int m : {1, 2, 4, 8, 15})
+        {
+            const int per_sm = tail_blocks_per_sm(m);
+            tail_grid_[m] = (per_sm >= 1 && sms >= 2 * kTailQueries && sms <= kTailMaxBlocks) ? sms : 0;
+        }
+    tail_max_samples_ = 2u * (uint32_t)sms * (uint32_t)kTailThreads;
     Sched s;
     std::memset(&s, 0, sizeof(s));
     s.prop_tile = block;
@@ -530,6 +547,7 @@ kgmt_status Engine::set_active(uint32_t n_active)
             set_error("set_active: more slots than the engine holds");
             return KGMT_ERR_INVALID_ARG;
         }
+    n_active_ = n_active;
     // by value through a kernel parameter: no host memory to keep alive, no wait
     k_set_n_slots<<<1, 1, 0, stream_>>>(d_sched_, n_active);
     KGMT_CUDA(cudaGetLastError(), "k_set_n_slots");
@@ -597,6 +615,44 @@ void Engine::reset_counters()
     launches_ = 0;
     prof_used_ = 0;
     prof_kind_.clear();
+    tail_iters_ = 0;
+    // the two counters are adjacent: one memset
+    if(d_tail_) cudaMemsetAsync(&d_tail_->fp32_ops, 0, 2 * sizeof(unsigned long long), stream_);
+}
+
+kgmt_status Engine::tail_counters(uint32_t* iterations, uint64_t* fp32_ops, uint64_t* samples)
+{
+    unsigned long long v[2] = {0, 0};
+    KGMT_CUDA(cudaMemcpyAsync(v, &d_tail_->fp32_ops, sizeof(v), cudaMemcpyDeviceToHost, stream_), "download(tail)");
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    *iterations = tail_iters_;
+    *fp32_ops = v[0];
+    *samples = v[1];
+    return KGMT_OK;
+}
+
+kgmt_status Engine::run_tail(bool* done, bool* declined_at_once)
+{
+    NvtxRange r("kgmt tail launch");
+    if(profile_)
+        {
+            kgmt_status st = record_event(nullptr);
+            if(st != KGMT_OK) return st;
+            prof_kind_.push_back(1);
+        }
+    KGMT_CUDA(launch_tail(args(), d_tail_, models_, tail_grid_[models_], smem_boxes_, tail_max_samples_, d_running_ + 2, stream_), "k_tail");
+    if(profile_)
+        {
+            kgmt_status st = record_event(nullptr);
+            if(st != KGMT_OK) return st;
+        }
+    launches_ += 1;
+    KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    volatile uint32_t* w = h_running_;
+    tail_iters_ += w[2];
+    *done = w[0] == 0u;
+    *declined_at_once = w[3] != 0u && w[2] == 0u;
+    return KGMT_OK;
 }
 
 kgmt_status Engine::kernel_times(float ms[3], uint32_t n[3])
@@ -663,11 +719,25 @@ kgmt_status Engine::run_until_done(uint32_t max_iters)
     // Units are launched one ahead of the poll: after unit u-1 completes, the
     // running count the last schedule wrote (unit u-1's or a later one's) is
     // read from the mapped host word; nothing but the event record sits in
-    // the stream between two graph replays.
+    // the stream between two graph replays.  Once at most kTailQueries
+    // queries run, one persistent tail launch takes the iterations left (it
+    // hands back to the units when an iteration outgrows it; after a launch
+    // that could not take even one iteration, the next attempt waits twice as
+    // many units).
     NvtxRange r("kgmt run until done");
     const uint32_t G = iters_per_graph_;
     const uint32_t max_units = (max_iters + G - 1) / G + 2;
     volatile uint32_t* running = h_running_;
+    const bool tail = tail_on_ && tail_grid_[models_] > 0;
+    uint32_t backoff = 1, wait_units = 0;
+    if(tail && n_active_ <= (uint32_t)kTailQueries)
+        {
+            bool done = false, at_once = false;
+            kgmt_status st = run_tail(&done, &at_once);
+            if(st != KGMT_OK) return st;
+            if(done) return KGMT_OK;
+            if(at_once) wait_units = backoff, backoff *= 2;
+        }
     for(uint32_t u = 0; u < max_units; ++u)
         {
             kgmt_status st = launch_unit();
@@ -676,7 +746,17 @@ kgmt_status Engine::run_until_done(uint32_t max_iters)
             if(u > 0)
                 {
                     KGMT_CUDA(cudaEventSynchronize(ev_[(u - 1) & 1]), "cudaEventSynchronize");
-                    if(*running == 0) break;
+                    const uint32_t n = *running;
+                    if(n == 0) break;
+                    if(wait_units > 0) --wait_units;
+                    else if(tail && n <= (uint32_t)kTailQueries)
+                        {
+                            bool done = false, at_once = false;
+                            st = run_tail(&done, &at_once);
+                            if(st != KGMT_OK) return st;
+                            if(done) break;
+                            if(at_once) wait_units = backoff, backoff *= 2;
+                        }
                 }
         }
     KGMT_CUDA(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");

@@ -119,10 +119,19 @@ class Engine {
     void add_launches(uint64_t n) { launches_ += n; }
     uint64_t launches() const { return launches_; }
     // sums the event pairs recorded since reset_counters (call after a sync)
+    // kinds: 0 propagate, 1 tail launch, 2 append
     kgmt_status kernel_times(float ms[3], uint32_t n[3]);
+    // the persistent tail launch (kgmt_tail.cuh) for the last few running
+    // queries in run_until_done; on by default, KGMT_TAIL=0 turns it off
+    void set_tail(bool on) { tail_on_ = on; }
+    // iterations and algorithmic FP32 operations of the tail launches since
+    // reset_counters (call after a sync)
+    kgmt_status tail_counters(uint32_t* iterations, uint64_t* fp32_ops, uint64_t* samples);
 
    private:
     kgmt_status launch_iteration();
+    // one tail launch after what is queued, waited for; *done: nothing runs any more
+    kgmt_status run_tail(bool* done, bool* declined_at_once);
     kgmt_status record_event(cudaEvent_t* out);
     kgmt_status launch_unit();
     kgmt_status build_graph();
@@ -143,7 +152,8 @@ class Engine {
     uint32_t* d_tile_a_ = nullptr;
     uint32_t* d_tile_c_ = nullptr;
     uint32_t* d_tile_old_ = nullptr;
-    uint32_t* h_running_ = nullptr;  // mapped pinned host words: [0] Sched::host_running, [1] error readback
+    uint32_t* h_running_ = nullptr;  // mapped pinned host words: [0] Sched::host_running, [1] error readback,
+                                     // [2] tail iterations, [3] tail stopped for size
     QueryState* h_stage_states_ = nullptr;  // pinned staging for state readbacks
     uint32_t* d_running_ = nullptr;  // its device address
     cudaEvent_t ev_[2] = {nullptr, nullptr};
@@ -152,6 +162,12 @@ class Engine {
     uint32_t iters_launched_ = 0;
     uint64_t launches_ = 0;
     bool profile_ = false;
+    bool tail_on_ = true;
+    TailScratch* d_tail_ = nullptr;
+    int tail_grid_[16] = {};          // tail launch grid per propagate variant (0: unavailable)
+    uint32_t tail_max_samples_ = 0;   // largest iteration the tail launch takes
+    uint32_t n_active_ = 0;           // slots the kernels look at
+    uint32_t tail_iters_ = 0;
     std::vector<cudaEvent_t> prof_events_;  // pool, pairs (start, stop)
     std::vector<int> prof_kind_;            // kernel of each pair
     size_t prof_used_ = 0;

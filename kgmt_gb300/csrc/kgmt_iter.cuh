@@ -444,8 +444,11 @@ __device__ __forceinline__ bool propagate_model(const QueryParams& p, const Grid
 }
 
 // rows of D floats: with D even every row starts 8-byte aligned (row
-// buffers are 256-byte aligned), so they move as float2 pairs
-template <int D>
+// buffers are 256-byte aligned), so they move as float2 pairs.  COHERENT:
+// the row may have been written earlier in the same launch by another block
+// (the persistent tail kernel), so it is read through L2 instead of the
+// read-only path, which is only valid for data no one writes during the launch.
+template <int D, bool COHERENT = false>
 __device__ __forceinline__ void load_row_ro(const float* __restrict__ src, float* r)
 {
     if constexpr(D % 2 == 0)
@@ -453,14 +456,14 @@ __device__ __forceinline__ void load_row_ro(const float* __restrict__ src, float
 #pragma unroll
             for(int c = 0; c < D / 2; ++c)
                 {
-                    const float2 v = __ldg((const float2*)src + c);
+                    const float2 v = COHERENT ? __ldcg((const float2*)src + c) : __ldg((const float2*)src + c);
                     r[2 * c] = v.x, r[2 * c + 1] = v.y;
                 }
         }
     else
         {
 #pragma unroll
-            for(int c = 0; c < D; ++c) r[c] = __ldg(src + c);
+            for(int c = 0; c < D; ++c) r[c] = COHERENT ? __ldcg(src + c) : __ldg(src + c);
         }
 }
 
@@ -501,7 +504,7 @@ __device__ __forceinline__ int sample_steps(const QueryParams& p, const U4& kb)
 
 // gather the parent row and draw the sample's uniforms (no obstacle access,
 // so it runs while the tile's boxes are still in flight); kb: its key block
-template <int MODEL>
+template <int MODEL, bool COHERENT = false>
 __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const PropCtx& c, uint32_t s, const U4& kb, float* x0, float* u)
 {
     constexpr int D = ModelDims<MODEL>::D;
@@ -509,7 +512,7 @@ __device__ __forceinline__ uint32_t prepare_sample(const QueryParams& p, const P
     uint32_t par = e < c.n_react ? (KGMT_BOUND(e < p.capacity) ? p.rep_old[e] : 0u)
                                  : (KGMT_BOUND(e - c.n_react < p.capacity) ? p.rep_new[e - c.n_react] : 0u);
     if(!KGMT_BOUND(par < p.capacity)) par = 0u;
-    load_row_ro<D>(p.tree + (size_t)par * D, x0);
+    load_row_ro<D, COHERENT>(p.tree + (size_t)par * D, x0);
     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
     constexpr bool four = ModelDims<MODEL>::NC == 4;
     const U4 other = philox4x32_10(s, c.itr, 0u, four ? 0u : 1u, k0, k1);
@@ -586,8 +589,9 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
 // every thread gets about the same work and a warp's lanes loop about equally
 // long in each pass.  `wait` runs once, after pass 0 has gathered its parents
 // and draws (the boxes' bulk copy may be in flight until then).
-// Block-uniform call.
-template <int NT, int MODELS, typename Wait>
+// Block-uniform call.  COHERENT: parent rows may have been appended by other
+// blocks earlier in the same launch (see load_row_ro).
+template <int NT, int MODELS, bool COHERENT = false, typename Wait>
 __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const PropCtx& sc, uint32_t lt, uint32_t tile, uint32_t smem_boxes, PropShared* sh,
                                                uint32_t* s_hist, uint32_t* s_perm, uint4* s_key, const float4* s_obs, const uint16_t* s_gstart,
                                                const uint16_t* s_gitems, const uint32_t* s_gmeta, Wait&& wait)
@@ -657,12 +661,39 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
                 {
                     const uint4 k4 = s_key[slot];
                     const U4 kb1{k4.x, k4.y, k4.z, k4.w};
-                    with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value>(sp, sc, s, kb1, x0, u); });
+                    with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value, COHERENT>(sp, sc, s, kb1, x0, u); });
                 }
             if(pass == 0) wait();
             const GridView grid{(sp.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, sp.grid_items};
             with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(sp, grid, obs, sp.n_obstacles, s, live, par, x0, u, sh); });
         }
+}
+
+// Samples [s0, s0 + n) of one query, one per thread (n <= NT), in index
+// order -- no sort: with one such range per block the time of a launch is its
+// slowest warp's, which ordering the samples inside a block cannot shorten.
+// Parent rows are read coherently (they may have been appended by other
+// blocks in the same launch).  `wait` runs once, after the parents and draws
+// are gathered.  Block-uniform call.
+template <int NT, int MODELS, typename Wait>
+__device__ __forceinline__ void propagate_range(const QueryParams& sp, const PropCtx& sc, uint32_t s0, uint32_t n, uint32_t smem_boxes,
+                                                PropShared* sh, const float4* s_obs, const uint16_t* s_gstart, const uint16_t* s_gitems,
+                                                const uint32_t* s_gmeta, Wait&& wait)
+{
+    const int model = sp.model;
+    const uint32_t s = s0 + threadIdx.x;
+    const bool live = threadIdx.x < n && s < sc.n_samples;
+    float x0[KGMT_MAX_SAMPLE_DIM], u[8];
+    uint32_t par = 0;
+    if(live)
+        with_model<MODELS>(model, [&](auto m) {
+            const U4 kb = sample_key_block<decltype(m)::value>(sp, sc, s);
+            par = prepare_sample<decltype(m)::value, true>(sp, sc, s, kb, x0, u);
+        });
+    wait();
+    const float4* obs = sp.n_obstacles <= smem_boxes ? s_obs : sp.obstacles;
+    const GridView grid{(sp.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, sp.grid_items};
+    with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(sp, grid, obs, sp.n_obstacles, s, live, par, x0, u, sh); });
 }
 
 // Graph::updateVertices (Graph.cu:311-358) for one query, by one block: all
@@ -832,22 +863,23 @@ __device__ inline void finalize_query(const QueryParams& p, QueryState& st, Sche
 // registers before the first store: the two buffers might alias as far as
 // the compiler can tell, so interleaved loads would each wait for the
 // previous store's turn.
-template <int D>
+template <int D, bool COHERENT = false>
 __device__ __forceinline__ float append_row_d(const QueryParams& p, const float* src, float* dst)
 {
     float r[D];
-    load_row_ro<D>(src, r);
+    load_row_ro<D, COHERENT>(src, r);
     store_row<D>(dst, r);
     return goal_distance(p, r);
 }
 
+template <bool COHERENT = false>
 __device__ __forceinline__ float append_row(const QueryParams& p, const float* src, float* dst, int D)
 {
     switch(D)
         {
-            case 7: return append_row_d<7>(p, src, dst);
-            case 17: return append_row_d<17>(p, src, dst);
-            default: return append_row_d<10>(p, src, dst);
+            case 7: return append_row_d<7, COHERENT>(p, src, dst);
+            case 17: return append_row_d<17, COHERENT>(p, src, dst);
+            default: return append_row_d<10, COHERENT>(p, src, dst);
         }
 }
 

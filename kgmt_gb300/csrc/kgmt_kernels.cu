@@ -32,6 +32,7 @@
 #include <type_traits>
 
 #include "kgmt_iter.cuh"
+#include "kgmt_tail.cuh"
 
 namespace kgmt {
 
@@ -852,6 +853,76 @@ cudaError_t launch_stage_obstacles(const float* src, float4* dst, uint32_t n, in
     if(n == 0) return cudaSuccess;
     k_stage_obstacles<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n, ws_dims == 2 ? 2 : 3);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// persistent tail launch
+// ---------------------------------------------------------------------------
+size_t tail_scratch_bytes() { return sizeof(TailScratch); }
+
+template <int MODELS>
+static int tail_occupancy_t()
+{
+    int n = 0;
+    if(cudaFuncSetAttribute(k_tail<MODELS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPropSmemBytes) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return 0;
+        }
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tail<MODELS>, kTailThreads, kPropSmemBytes) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return 0;
+        }
+    return n;
+}
+
+int tail_blocks_per_sm(int models)
+{
+    switch(models)
+        {
+            case kBitDI: return tail_occupancy_t<kBitDI>();
+            case kBitQuad: return tail_occupancy_t<kBitQuad>();
+            case kBitDubins: return tail_occupancy_t<kBitDubins>();
+            case kBitUnicycle: return tail_occupancy_t<kBitUnicycle>();
+            default: return tail_occupancy_t<kAllModels>();
+        }
+}
+
+template <int MODELS>
+static cudaError_t launch_tail_t(const LaunchArgs& a, TailScratch* ts, int grid, uint32_t boxes, uint32_t max_samples, uint32_t* host_words,
+                                 cudaStream_t s)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid, 1, 1);
+    cfg.blockDim = dim3((unsigned)kTailThreads, 1, 1);
+    cfg.dynamicSmemBytes = prop_smem_bytes(boxes);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_tail<MODELS>, a.params, a.states, a.sched, ts, a.tile_a_base, a.tile_c_base, a.tile_c_old, boxes,
+                              max_samples, host_words);
+}
+
+cudaError_t launch_tail(const LaunchArgs& a, TailScratch* ts, int models, int grid, uint32_t smem_boxes, uint32_t max_samples,
+                        uint32_t* host_words, cudaStream_t s)
+{
+    if(grid < 2 * kTailQueries || grid > kTailMaxBlocks) return cudaErrorInvalidValue;
+    const uint32_t boxes = smem_boxes < kSmemBoxesMin ? kSmemBoxesMin : smem_boxes > (uint32_t)kSmemObstacles ? (uint32_t)kSmemObstacles : smem_boxes;
+    // the barrier counter starts each launch at zero
+    cudaError_t e = cudaMemsetAsync(&ts->bar, 0, sizeof(uint32_t), s);
+    if(e != cudaSuccess) return e;
+    switch(models)
+        {
+            case kBitDI: return launch_tail_t<kBitDI>(a, ts, grid, boxes, max_samples, host_words, s);
+            case kBitQuad: return launch_tail_t<kBitQuad>(a, ts, grid, boxes, max_samples, host_words, s);
+            case kBitDubins: return launch_tail_t<kBitDubins>(a, ts, grid, boxes, max_samples, host_words, s);
+            case kBitUnicycle: return launch_tail_t<kBitUnicycle>(a, ts, grid, boxes, max_samples, host_words, s);
+            default: return launch_tail_t<kAllModels>(a, ts, grid, boxes, max_samples, host_words, s);
+        }
 }
 
 cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, const float* u, const float* obs, uint32_t n_obs, uint32_t n,

@@ -35,4 +35,14 @@ cudaError_t launch_propagate_samples(const QueryParams& p, const float* x0, cons
 int propagate_blocks_per_sm(int block, int models);
 int append_blocks_per_sm();
 
+// persistent tail launch (kgmt_tail.cuh): whole iterations for at most
+// kTailQueries running queries in one cooperative launch of `grid` blocks;
+// stops before an iteration of more than max_samples samples.  host_words
+// (mapped, or null): [0] iterations run, [1] 1 if it stopped for size.
+size_t tail_scratch_bytes();
+// blocks of the tail kernel one SM holds (0: it cannot run)
+int tail_blocks_per_sm(int models);
+cudaError_t launch_tail(const LaunchArgs& a, TailScratch* ts, int models, int grid, uint32_t smem_boxes, uint32_t max_samples,
+                        uint32_t* host_words, cudaStream_t s);
+
 }  // namespace kgmt

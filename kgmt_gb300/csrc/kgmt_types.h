@@ -40,6 +40,12 @@ constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a device-side wait gi
 
 constexpr uint32_t kSlotEmpty = 0xFFFFFFFFu;  // QueryState::status of a never-admitted slot
 
+// persistent tail launch (kgmt_tail.cuh): at most this many running queries,
+// one block of kTailThreads per SM, at most kTailMaxBlocks blocks
+constexpr int kTailQueries = 4;
+constexpr int kTailThreads = 256;
+constexpr int kTailMaxBlocks = 1024;
+
 // static FP32 lane-operation counts per RK4 step, from the code in
 // kgmt_device.cuh (a multiply, add, fused multiply-add, divide or compare is
 // one; the quadrotor's portable sine/cosine counted as the operations it is
@@ -90,6 +96,7 @@ constexpr uint32_t kErrLookbackTimeout = 1u;
 constexpr uint32_t kErrCopyTimeout = 2u;
 constexpr uint32_t kErrBounds = 4u;  // an index check of a KGMT_CHECK_BOUNDS build failed
 constexpr uint32_t kErrAppendMismatch = 8u;  // appended samples != accepted samples
+constexpr uint32_t kErrBarrierTimeout = 16u;  // a grid-wide barrier of the tail launch gave up
 
 struct QueryParams {
     int32_t model;
@@ -198,6 +205,21 @@ struct Sched {
     // mapped pinned host word that mirrors `running` (or null): the host polls
     // it without a copy in the stream between graph replays
     uint32_t* host_running;
+};
+
+// device-side scratch of the persistent tail launch (kgmt_tail.cuh), one per engine
+struct TailScratch {
+    uint32_t bar;         // grid-barrier arrivals of the running launch (zeroed before it)
+    uint32_t iterations;  // iterations the last launch ran
+    uint32_t declined;    // 1: the last launch stopped before an iteration larger than it takes
+    uint32_t pad;
+    unsigned long long fp32_ops;  // algorithmic FP32 operations of the tail's propagation (host-zeroed)
+    unsigned long long samples;   // samples the tail propagated (host-zeroed)
+    uint32_t n_next[2][kTailQueries];                 // accepted samples per query, by iteration parity
+    uint32_t goal[2][kTailQueries];                   // smallest new goal-ball index per query (~0u: none)
+    uint32_t old_cnt[kTailQueries][kTailMaxBlocks];   // re-activated nodes of each block's chunk
+    uint32_t acc_cnt[kTailQueries][kTailMaxBlocks];   // accepted samples of each block's chunk
+    uint32_t rep_cnt[kTailQueries][kTailMaxBlocks];   // frontier entries (repeats) of each block's chunk
 };
 
 }  // namespace kgmt
