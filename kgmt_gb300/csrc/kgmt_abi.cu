@@ -654,7 +654,19 @@ extern "C" kgmt_status kgmt_batch_autotune_full(kgmt_batch* b, uint32_t n, const
 
 // ---------------------------------------------------------------------------
 // server: continuous batching with memory-based admission
+//
+// A step is asynchronous: it finishes the previous step (waits for its
+// iterations and for the copy of the states queued behind them, then retires
+// the queries they finished), admits queued queries into free slots, queues
+// this step's iterations (a CUDA-graph replay) and the copy of the states
+// behind them, and returns while the GPU runs.  Admission copies from pinned
+// staging and admits every new query with one kernel launch.  Queries that
+// fit may pass a head that does not (memory), within a window, until the head
+// has waited kMaxBypass steps; then nothing passes it.
 // ---------------------------------------------------------------------------
+constexpr uint32_t kAdmitWindow = 64;  // queued queries one step looks at
+constexpr uint32_t kMaxBypass = 16;    // steps the head may be passed before it blocks the queue
+
 struct PendingQuery {
     uint64_t ticket;
     kgmt_config cfg;
@@ -662,6 +674,7 @@ struct PendingQuery {
     float goal[KGMT_MAX_SAMPLE_DIM];
     std::vector<float> obstacles;
     std::chrono::steady_clock::time_point submitted;
+    uint32_t passed = 0;  // steps in which a later query was admitted before it
 };
 
 struct ResidentQuery {
@@ -672,6 +685,33 @@ struct ResidentQuery {
     std::chrono::steady_clock::time_point submitted;
 };
 
+// pinned host memory that grows geometrically, keeping its contents
+struct PinnedBuffer {
+    char* p = nullptr;
+    size_t cap = 0;
+    ~PinnedBuffer()
+    {
+        if(p) cudaFreeHost(p);
+    }
+    // no copy from the old buffer may be in flight when it grows
+    kgmt_status reserve(size_t bytes, size_t keep)
+    {
+        if(bytes <= cap) return KGMT_OK;
+        size_t n = cap ? cap : 65536;
+        while(n < bytes) n *= 2;
+        char* q = nullptr;
+        CHECK_ST(cuda_status(cudaMallocHost((void**)&q, n), "cudaMallocHost(staging)"));
+        if(p)
+            {
+                if(keep) std::memcpy(q, p, keep);
+                cudaFreeHost(p);
+            }
+        p = q;
+        cap = n;
+        return KGMT_OK;
+    }
+};
+
 struct kgmt_server {
     Engine eng;
     DeviceArena arena;
@@ -679,10 +719,24 @@ struct kgmt_server {
     std::deque<PendingQuery> queue;
     std::vector<ResidentQuery> slots;
     std::deque<kgmt_result> done;
-    std::vector<QueryState> states;
     uint64_t next_ticket = 1;
-    uint32_t running = 0;
-    bool resched = false;  // a resident query was cancelled: the next step recomputes the schedule
+    uint32_t resident = 0;     // admitted and not yet retired
+    uint32_t box_capacity = 0; // boxes a propagate block stages: the largest admitted so far
+    bool resched = false;      // a resident query was cancelled: the next step recomputes the schedule
+    // the step in flight: its iterations and the copy of states [0, copied)
+    bool inflight = false;
+    uint32_t copied = 0;
+    cudaEvent_t ev = nullptr;
+    QueryState* h_states = nullptr;  // pinned [max_slots]
+    uint32_t* h_error = nullptr;     // pinned
+    PinnedBuffer stage;              // params, raw boxes and the slot list of one admission
+    ~kgmt_server()
+    {
+        if(eng.stream()) cudaStreamSynchronize(eng.stream());
+        if(ev) cudaEventDestroy(ev);
+        if(h_states) cudaFreeHost(h_states);
+        if(h_error) cudaFreeHost(h_error);
+    }
 };
 
 extern "C" kgmt_status kgmt_server_create(const kgmt_server_options* opt, void* stream, kgmt_server** out)
@@ -695,16 +749,19 @@ extern "C" kgmt_status kgmt_server_create(const kgmt_server_options* opt, void* 
     RETURN_IF(!s, KGMT_ERR_OOM, "kgmt_server_create: host allocation failed");
     s->opt = *opt;
     if(s->opt.iters_per_step == 0) s->opt.iters_per_step = 1;
-    kgmt_status st = s->eng.init(opt->max_slots, (cudaStream_t)stream, opt->propagate_block ? opt->propagate_block : 256, 1, false);
+    // one graph replay per step: a unit of iters_per_step iterations
+    kgmt_status st = s->eng.init(opt->max_slots, (cudaStream_t)stream, opt->propagate_block ? opt->propagate_block : 256, s->opt.iters_per_step, true);
     if(st == KGMT_OK) st = s->arena.reserve(opt->memory_budget);
     if(st == KGMT_OK) st = s->eng.set_active(opt->max_slots);
+    if(st == KGMT_OK) st = cuda_status(cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming), "cudaEventCreate");
+    if(st == KGMT_OK) st = cuda_status(cudaMallocHost((void**)&s->h_states, sizeof(QueryState) * opt->max_slots), "cudaMallocHost(states)");
+    if(st == KGMT_OK) st = cuda_status(cudaMallocHost((void**)&s->h_error, sizeof(uint32_t)), "cudaMallocHost(error)");
     if(st != KGMT_OK)
         {
             delete s;
             return st;
         }
     s->slots.resize(opt->max_slots);
-    s->states.resize(opt->max_slots);
     *out = s;
     return KGMT_OK;
 }
@@ -735,83 +792,133 @@ extern "C" kgmt_status kgmt_server_submit(kgmt_server* s, const kgmt_config* cfg
     return KGMT_OK;
 }
 
+// waits for the step in flight and retires the queries it finished
+static kgmt_status server_finish_step(kgmt_server* s)
+{
+    if(!s->inflight) return KGMT_OK;
+    s->inflight = false;
+    CHECK_ST(cuda_status(cudaEventSynchronize(s->ev), "cudaEventSynchronize"));
+    const auto now = std::chrono::steady_clock::now();
+    for(uint32_t i = 0; i < s->copied; ++i)
+        {
+            ResidentQuery& r = s->slots[i];
+            if(!r.used) continue;
+            const QueryState& qs = s->h_states[i];
+            if(qs.status == KGMT_QUERY_RUNNING) continue;
+            kgmt_result res = to_result(qs, r.ticket);
+            res.latency_ms = (float)(std::chrono::duration<double, std::milli>(now - r.submitted).count());
+            s->done.push_back(res);
+            s->arena.release(r.offset);
+            r.used = false;
+            --s->resident;
+        }
+    const uint32_t err = *s->h_error;
+    RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "server: a device-side wait gave up (error bits " + std::to_string(err) + ")");
+    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "server: an index check failed (bounds-checked build)");
+    return KGMT_OK;
+}
+
 extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uint32_t* n_queued)
 {
     RETURN_IF(!s, KGMT_ERR_INVALID_ARG, "kgmt_server_step: NULL server");
+    CHECK_ST(server_finish_step(s));
     cudaStream_t st = s->eng.stream();
-    // ---- admission: FIFO while a slot and memory are free ----
-    bool admitted = false;
+    // ---- admission: queued queries in order into free slots while memory
+    // allows; a query that does not fit may be passed by later ones.  Each
+    // admitted query's params and raw boxes go to pinned staging (the previous
+    // step's copies from it are complete) ----
+    struct Admit {
+        uint32_t slot;
+        size_t params_at, raw_at, raw_bytes;
+        float* d_raw;
+    };
+    std::vector<Admit> adm;
+    std::vector<size_t> taken;  // queue positions admitted
+    size_t used = 0;
     uint32_t slot = 0;
-    while(!s->queue.empty())
+    for(size_t pos = 0; pos < s->queue.size() && pos < kAdmitWindow; ++pos)
         {
             while(slot < s->slots.size() && s->slots[slot].used) ++slot;
             if(slot >= s->slots.size()) break;
-            PendingQuery& q = s->queue.front();
+            PendingQuery& q = s->queue[pos];
             const uint32_t n_obs = (uint32_t)(q.obstacles.size() / 6);
             const QueryLayout L = layout_of(q.cfg, n_obs, true);
             const size_t raw_at = (L.total + 255) & ~size_t(255);
             size_t off = 0;
-            if(!s->arena.alloc(raw_at + (size_t)n_obs * 24 + 256, &off)) break;  // wait for memory
+            if(!s->arena.alloc(raw_at + (size_t)n_obs * 24 + 256, &off))
+                {
+                    // it waits for memory; later queries may pass it unless it
+                    // is the head and has been passed kMaxBypass times
+                    if(pos == 0 && q.passed >= kMaxBypass) break;
+                    continue;
+                }
             char* chunk = s->arena.base() + off;
             QueryParams prm = make_params(q.cfg, q.init, q.goal, chunk, L, nullptr, n_obs);
-            if(n_obs)
-                {
-                    float* raw = (float*)(chunk + raw_at);
-                    CHECK_ST(cuda_status(cudaMemcpyAsync(raw, q.obstacles.data(), (size_t)n_obs * 24, cudaMemcpyHostToDevice, st),
-                                         "upload obstacles"));
-                    CHECK_ST(cuda_status(launch_stage_obstacles(raw, prm.obstacles, n_obs, 3, st), "stage obstacles"));
-                }
-            s->eng.host_params(slot) = prm;
-            CHECK_ST(s->eng.upload_params(slot, 1));
-            CHECK_ST(s->eng.init_slots(slot, 1));
+            prm.raw_obstacles = n_obs ? (const float*)(chunk + raw_at) : nullptr;
+            prm.raw_w = 3;
+            Admit a;
+            a.slot = slot;
+            a.params_at = (used + 15) & ~size_t(15);
+            a.raw_at = (a.params_at + sizeof(QueryParams) + 15) & ~size_t(15);
+            a.raw_bytes = (size_t)n_obs * 24;
+            a.d_raw = (float*)(chunk + raw_at);
+            CHECK_ST(s->stage.reserve(a.raw_at + a.raw_bytes, used));
+            std::memcpy(s->stage.p + a.params_at, &prm, sizeof(QueryParams));
+            if(a.raw_bytes) std::memcpy(s->stage.p + a.raw_at, q.obstacles.data(), a.raw_bytes);
+            used = a.raw_at + a.raw_bytes;
+            adm.push_back(a);
+            taken.push_back(pos);
+            for(size_t j = 0; j < pos; ++j) s->queue[j].passed += 1;
             ResidentQuery& r = s->slots[slot];
             r.used = true;
             r.model_bit = Engine::model_bit(q.cfg.model);
             r.ticket = q.ticket;
             r.offset = off;
             r.submitted = q.submitted;
-            s->queue.pop_front();
-            admitted = true;
-            ++s->running;
+            if(n_obs > s->box_capacity) s->box_capacity = n_obs;
+            ++s->resident;
+            ++slot;
         }
-    if(admitted || s->resched)
+    if(!adm.empty())
+        {
+            const size_t list_at = (used + 15) & ~size_t(15);
+            CHECK_ST(s->stage.reserve(list_at + sizeof(uint32_t) * adm.size(), used));
+            uint32_t* list = (uint32_t*)(s->stage.p + list_at);
+            for(size_t i = 0; i < adm.size(); ++i)
+                {
+                    const Admit& a = adm[i];
+                    list[i] = a.slot;
+                    CHECK_ST(s->eng.upload_params_async(a.slot, (const QueryParams*)(s->stage.p + a.params_at)));
+                    if(a.raw_bytes)
+                        CHECK_ST(cuda_status(cudaMemcpyAsync(a.d_raw, s->stage.p + a.raw_at, a.raw_bytes, cudaMemcpyHostToDevice, st),
+                                             "upload obstacles"));
+                }
+            CHECK_ST(s->eng.admit_slot_list(list, (uint32_t)adm.size()));
+            for(size_t i = taken.size(); i-- > 0;) s->queue.erase(s->queue.begin() + (std::ptrdiff_t)taken[i]);
+        }
+    if(!adm.empty() || s->resched)
         {
             int models = 0;
             for(size_t i = 0; i < s->slots.size(); ++i)
                 if(s->slots[i].used) models |= s->slots[i].model_bit;
             s->eng.set_models(models);
+            s->eng.set_max_obstacles(s->box_capacity);
             CHECK_ST(s->eng.schedule());
             s->resched = false;
         }
-    // ---- iterations for every resident query ----
-    if(s->running) CHECK_ST(s->eng.run_iterations(s->opt.iters_per_step));
-    // ---- retire finished queries ----
-    const uint32_t n = (uint32_t)s->slots.size();
-    CHECK_ST(s->eng.read_states(0, n, s->states.data()));
-    const auto now = std::chrono::steady_clock::now();
-    uint32_t running = 0;
-    for(uint32_t i = 0; i < n; ++i)
+    // ---- this step's iterations, and the states behind them ----
+    if(s->resident)
         {
-            ResidentQuery& r = s->slots[i];
-            if(!r.used) continue;
-            const QueryState& qs = s->states[i];
-            if(qs.status == KGMT_QUERY_RUNNING)
-                {
-                    ++running;
-                    continue;
-                }
-            kgmt_result res = to_result(qs, r.ticket);
-            res.latency_ms = (float)(std::chrono::duration<double, std::milli>(now - r.submitted).count());
-            s->done.push_back(res);
-            s->arena.release(r.offset);
-            r.used = false;
+            uint32_t hwm = 0;
+            for(uint32_t i = 0; i < (uint32_t)s->slots.size(); ++i)
+                if(s->slots[i].used) hwm = i + 1;
+            CHECK_ST(s->eng.launch_units(1));
+            CHECK_ST(s->eng.enqueue_state_copy(hwm, s->h_states, s->h_error));
+            CHECK_ST(cuda_status(cudaEventRecord(s->ev, st), "cudaEventRecord"));
+            s->copied = hwm;
+            s->inflight = true;
         }
-    s->running = running;
-    uint32_t err = 0;
-    CHECK_ST(s->eng.read_error(&err));
-    RETURN_IF(err != 0, KGMT_ERR_TIMEOUT, "server: a device-side wait gave up (error bits " + std::to_string(err) + ")");
-    RETURN_IF(bounds_error_take() != 0, KGMT_ERR_INTERNAL, "server: an index check failed (bounds-checked build)");
-    if(n_running) *n_running = running;
+    if(n_running) *n_running = s->resident;
     if(n_queued) *n_queued = (uint32_t)s->queue.size();
     return KGMT_OK;
 }
@@ -819,6 +926,9 @@ extern "C" kgmt_status kgmt_server_step(kgmt_server* s, uint32_t* n_running, uin
 extern "C" kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket)
 {
     RETURN_IF(!s, KGMT_ERR_INVALID_ARG, "kgmt_server_cancel: NULL server");
+    // no kernel of a step may run while a status is rewritten: finish the
+    // step in flight (its finished queries retire as in a step)
+    CHECK_ST(server_finish_step(s));
     const auto now = std::chrono::steady_clock::now();
     for(auto it = s->queue.begin(); it != s->queue.end(); ++it)
         if(it->ticket == ticket)
@@ -837,8 +947,8 @@ extern "C" kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket)
         {
             ResidentQuery& r = s->slots[i];
             if(!r.used || r.ticket != ticket) continue;
-            // no kernel runs between steps: the status is final before the
-            // next step's schedule, which then gives the slot no tiles
+            // the status is final before the next step's schedule, which then
+            // gives the slot no tiles
             CHECK_ST(s->eng.write_status(i, KGMT_QUERY_CANCELLED));
             QueryState qs;
             CHECK_ST(s->eng.read_states(i, 1, &qs));
@@ -847,7 +957,7 @@ extern "C" kgmt_status kgmt_server_cancel(kgmt_server* s, uint64_t ticket)
             s->done.push_back(res);
             s->arena.release(r.offset);
             r.used = false;
-            if(s->running) --s->running;
+            --s->resident;
             s->resched = true;
             return KGMT_OK;
         }

@@ -383,6 +383,7 @@ Engine::~Engine()
     cudaFree(d_tile_a_);
     cudaFree(d_tile_c_);
     cudaFree(d_tile_old_);
+    cudaFree(d_slot_list_);
     cudaFree(d_tail_);
     if(own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
@@ -427,6 +428,7 @@ kgmt_status Engine::init(uint32_t slots, cudaStream_t stream, uint32_t prop_bloc
     KGMT_CUDA(cudaMemsetAsync(d_tile_c_, 0, sizeof(uint32_t) * (slots + 1), stream_), "memset");
     KGMT_CUDA(cudaMemsetAsync(d_tile_old_, 0, sizeof(uint32_t) * slots, stream_), "memset");
     KGMT_CUDA(device_alloc((void**)&d_tail_, tail_scratch_bytes()), "cudaMalloc(tail)");
+    KGMT_CUDA(device_alloc((void**)&d_slot_list_, sizeof(uint32_t) * slots), "cudaMalloc(slot list)");
     KGMT_CUDA(cudaMemsetAsync(d_tail_, 0, tail_scratch_bytes(), stream_), "memset(tail)");
     {
         const char* e = std::getenv("KGMT_TAIL");
@@ -771,6 +773,55 @@ kgmt_status Engine::run_iterations(uint32_t iters)
             if(st != KGMT_OK) return st;
         }
     iters_launched_ += iters;
+    return KGMT_OK;
+}
+
+kgmt_status Engine::launch_units(uint32_t units)
+{
+    for(uint32_t u = 0; u < units; ++u)
+        {
+            kgmt_status st = launch_unit();
+            if(st != KGMT_OK) return st;
+        }
+    return KGMT_OK;
+}
+
+kgmt_status Engine::upload_params_async(uint32_t slot, const QueryParams* pinned)
+{
+    if(slot >= slots_)
+        {
+            set_error("upload_params_async: slot out of bounds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    h_params_[slot] = *pinned;
+    KGMT_CUDA(cudaMemcpyAsync(d_params_ + slot, pinned, sizeof(QueryParams), cudaMemcpyHostToDevice, stream_), "upload(params)");
+    return KGMT_OK;
+}
+
+kgmt_status Engine::admit_slot_list(const uint32_t* pinned_slots, uint32_t count)
+{
+    if(count == 0) return KGMT_OK;
+    if(count > slots_)
+        {
+            set_error("admit_slot_list: more slots than the engine holds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    KGMT_CUDA(cudaMemcpyAsync(d_slot_list_, pinned_slots, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, stream_), "upload(slots)");
+    KGMT_CUDA(launch_admit(args(), 0, count, stream_, d_slot_list_), "k_admit");
+    launches_ += 2;
+    return KGMT_OK;
+}
+
+kgmt_status Engine::enqueue_state_copy(uint32_t count, QueryState* pinned_states, uint32_t* pinned_error)
+{
+    if(count > slots_)
+        {
+            set_error("enqueue_state_copy: more slots than the engine holds");
+            return KGMT_ERR_INVALID_ARG;
+        }
+    if(count)
+        KGMT_CUDA(cudaMemcpyAsync(pinned_states, d_states_, sizeof(QueryState) * count, cudaMemcpyDeviceToHost, stream_), "download(states)");
+    KGMT_CUDA(cudaMemcpyAsync(pinned_error, &d_sched_->error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "download(error)");
     return KGMT_OK;
 }
 

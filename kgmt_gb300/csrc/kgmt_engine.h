@@ -86,8 +86,19 @@ class Engine {
     kgmt_status schedule();
     // runs iterations until no query is running (or max_iters + slack)
     kgmt_status run_until_done(uint32_t max_iters);
-    // runs exactly `iters` iterations (served loop)
+    // runs exactly `iters` iterations (direct launches)
     kgmt_status run_iterations(uint32_t iters);
+    // enqueues `units` units of iters_per_graph iterations (graph replays when
+    // graphs are on); returns without waiting
+    kgmt_status launch_units(uint32_t units);
+    // served admission, all enqueued without waiting: the params of one slot
+    // from pinned host memory; then the slots listed in pinned host memory
+    // admitted by one launch (their raw boxes staged by it)
+    kgmt_status upload_params_async(uint32_t slot, const QueryParams* pinned);
+    kgmt_status admit_slot_list(const uint32_t* pinned_slots, uint32_t count);
+    // enqueues copies of the states of slots [0, count) and of the error bits
+    // into pinned host memory (readable after the stream reaches them)
+    kgmt_status enqueue_state_copy(uint32_t count, QueryState* pinned_states, uint32_t* pinned_error);
     kgmt_status read_states(uint32_t first, uint32_t count, QueryState* out);
     // sets one slot's status on the device (between launches)
     kgmt_status write_status(uint32_t slot, uint32_t status);
@@ -152,6 +163,7 @@ class Engine {
     uint32_t* d_tile_a_ = nullptr;
     uint32_t* d_tile_c_ = nullptr;
     uint32_t* d_tile_old_ = nullptr;
+    uint32_t* d_slot_list_ = nullptr;  // [slots] slots of a served admission
     uint32_t* h_running_ = nullptr;  // mapped pinned host words: [0] Sched::host_running, [1] error readback,
                                      // [2] tail iterations, [3] tail stopped for size
     QueryState* h_stage_states_ = nullptr;  // pinned staging for state readbacks

@@ -141,14 +141,34 @@ cudaError_t launch_selftest_wait(unsigned long long* tiles, uint32_t* error, uin
     return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// admission: root node, cleared region tables, first frontier (root x5)
-// ---------------------------------------------------------------------------
-__global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32_t first, uint32_t count)
+// rows of 2W floats (min corner, max corner; W = 3, or 2 for the planar
+// model, whose z extents are then 0 and never tested) -> float4 pairs
+__device__ __forceinline__ void stage_box(const float* r, int w, float4* dst)
 {
-    const uint32_t q = first + blockIdx.x;
+    if(w == 2)
+        {
+            dst[0] = make_float4(r[0], r[1], 0.0f, 0.0f);
+            dst[1] = make_float4(r[2], r[3], 0.0f, 0.0f);
+        }
+    else
+        {
+            dst[0] = make_float4(r[0], r[1], r[2], 0.0f);
+            dst[1] = make_float4(r[3], r[4], r[5], 0.0f);
+        }
+}
+
+// ---------------------------------------------------------------------------
+// admission: root node, cleared region tables, first frontier (root x5); the
+// slots are [first, first + count), or slots[0 .. count) when a list is given
+// ---------------------------------------------------------------------------
+__global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32_t first, uint32_t count, const uint32_t* __restrict__ slots)
+{
     if(blockIdx.x >= count) return;
+    const uint32_t q = slots ? slots[blockIdx.x] : first + blockIdx.x;
     const QueryParams& p = P[q];
+    if(p.raw_obstacles)
+        for(uint32_t o = threadIdx.x; o < p.n_obstacles; o += blockDim.x)
+            stage_box(p.raw_obstacles + (size_t)o * 2 * p.raw_w, p.raw_w, p.obstacles + 2 * o);
     for(uint32_t r = threadIdx.x; r < p.regions; r += blockDim.x)
         {
             p.counter[r] = 0;
@@ -192,13 +212,14 @@ __global__ void k_admit(const QueryParams* __restrict__ P, QueryState* S, uint32
 // 16-bit indices hold, or more entries than the budget leave the grid marked
 // unusable and the propagate kernel tests every box.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restrict__ P, uint32_t first, uint32_t count)
+__global__ void __launch_bounds__(256) k_build_grid(const QueryParams* __restrict__ P, uint32_t first, uint32_t count,
+                                                    const uint32_t* __restrict__ slots)
 {
     __shared__ uint32_t cnt[kGridCells];
     __shared__ uint32_t scratch[34];
     __shared__ int s_bad;
     if(blockIdx.x >= count) return;
-    const QueryParams& p = P[first + blockIdx.x];
+    const QueryParams& p = P[slots ? slots[blockIdx.x] : first + blockIdx.x];
     if(p.grid_start == nullptr) return;
     const uint32_t n = p.n_obstacles;
     for(uint32_t i = threadIdx.x; i < kGridCells; i += blockDim.x) cnt[i] = 0;
@@ -667,22 +688,6 @@ __global__ void k_paths(const QueryParams* __restrict__ P, QueryState* S, uint32
 // ---------------------------------------------------------------------------
 // obstacles: [n][6] rows (min xyz, max xyz) -> [n][2] float4 in the arena
 // ---------------------------------------------------------------------------
-// rows of 2W floats (min corner, max corner; W = 3, or 2 for the planar
-// model, whose z extents are then 0 and never tested) -> float4 pairs
-__device__ __forceinline__ void stage_box(const float* r, int w, float4* dst)
-{
-    if(w == 2)
-        {
-            dst[0] = make_float4(r[0], r[1], 0.0f, 0.0f);
-            dst[1] = make_float4(r[2], r[3], 0.0f, 0.0f);
-        }
-    else
-        {
-            dst[0] = make_float4(r[0], r[1], r[2], 0.0f);
-            dst[1] = make_float4(r[3], r[4], r[5], 0.0f);
-        }
-}
-
 __global__ void k_stage_obstacles(const float* __restrict__ src, float4* dst, uint32_t n, int w)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -825,13 +830,13 @@ cudaError_t launch_append(const LaunchArgs& a, int grid, cudaStream_t s)
     return cudaLaunchKernelEx(&cfg, k_append, a.params, a.states, a.sched, a.tile_a_base, a.tile_c_base, a.tile_c_old);
 }
 
-cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s)
+cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s, const uint32_t* slots)
 {
     if(count == 0) return cudaSuccess;
-    k_admit<<<count, 256, 0, s>>>(a.params, a.states, first, count);
+    k_admit<<<count, 256, 0, s>>>(a.params, a.states, first, count, slots);
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return e;
-    k_build_grid<<<count, 256, 0, s>>>(a.params, first, count);
+    k_build_grid<<<count, 256, 0, s>>>(a.params, first, count, slots);
     return cudaGetLastError();
 }
 

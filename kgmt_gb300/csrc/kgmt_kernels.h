@@ -15,7 +15,8 @@ struct LaunchArgs {
     uint32_t* tile_c_old;   // [slots]
 };
 
-cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s);
+// admits slots [first, first + count), or slots[0 .. count) (device memory) when given
+cudaError_t launch_admit(const LaunchArgs& a, uint32_t first, uint32_t count, cudaStream_t s, const uint32_t* slots = nullptr);
 cudaError_t launch_schedule(const LaunchArgs& a, cudaStream_t s);
 // models: bit 0 double integrator, bit 1 quadrotor (the mix the launch may meet)
 // smem_boxes: boxes a block stages in shared memory (the largest query of the

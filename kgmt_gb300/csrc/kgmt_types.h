@@ -152,6 +152,11 @@ struct QueryParams {
     float grid_scale;        // grid_dim / workspace size
     uint32_t grid_budget;    // capacity of grid_items (<= 65535)
     uint32_t* grid_meta;     // [4]: [0] items in use, [1] 1 = usable
+    // boxes as rows of 2 * raw_w floats (min corner, max corner) in device
+    // memory, staged into `obstacles` by the admission kernel (served queries;
+    // null when staged beforehand)
+    const float* raw_obstacles;
+    int32_t raw_w;
     uint16_t* grid_start;    // [grid_dim^3 + 1] CSR starts (16-bit: at most 65535 items)
     uint16_t* grid_items;    // [grid_budget] box indices, cell by cell
 };

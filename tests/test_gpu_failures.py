@@ -177,12 +177,14 @@ except _abi.KgmtError as e:
 '''
 
 
-@pytest.mark.parametrize("after,expect", [(0, "error 2"), (2, "error 2"), (5, "error 2"), (6, "error 2"), (1000, "planned True")])
+@pytest.mark.parametrize("after,expect", [(0, "error 2"), (2, "error 2"), (5, "error 2"), (7, "error 2"), (8, "error 2"),
+                                          (1000, "planned True")])
 def test_injected_allocation_failure_is_an_error_not_a_crash(lib, after, expect):
     """KGMT_FAULT_ALLOC_AFTER=n makes the library's (n+1)-th device
     allocation fail as out of memory without reaching the driver (a host-side
-    injector): creating the batch engine (allocations 0-5) or growing its
-    arena while planning (6) then raises KGMT_ERR_OOM and the process exits
+    injector): creating the batch engine (allocations 0-7: descriptors, tile
+    bases, the tail launch's scratch, the admission slot list) or growing its
+    arena while planning (8) then raises KGMT_ERR_OOM and the process exits
     cleanly; with no failure in reach the batch plans as the oracle does."""
     import os
     import subprocess

@@ -445,6 +445,36 @@ def test_server_results_same_alone_and_in_mix():
             assert got[i][k] == ref[k], (i, k, got[i][k], ref[k])
 
 
+def test_server_lets_small_queries_pass_a_head_that_does_not_fit():
+    """Admission by device memory with passing: four small queries fill part
+    of a 20 MiB budget, a large one (T = 150k, 15.5 MiB) queued behind them
+    does not fit, and four more small ones queued behind it are admitted
+    first; the large one runs once memory frees up.  Every result is the
+    oracle's (each query alone), whatever order the queries ran in."""
+    from kgmt_gb300.planner import Server
+    small = W.double_integrator_batch(8, seed=14, tree_capacity=20_000)
+    big = W.double_integrator_batch(1, seed=15, tree_capacity=150_000)[0]
+    order = small[:4] + [big] + small[4:]
+    srv = Server(max_slots=16, memory_budget=20 << 20, iters_per_step=2)
+    tickets = [srv.submit(q.config, q.init, q.goal, q.obstacles) for q in order]
+    got, finished = {}, []
+    for _ in range(5000):
+        srv.step()
+        for r in srv.poll():
+            got[r["ticket"]] = r
+            finished.append(r["ticket"])
+        if len(got) == len(order):
+            break
+    refs = O.plan_batch(order)
+    for t, ref in zip(tickets, refs):
+        for k in ("status", "iterations", "tree_size", "goal_index", "samples_drawn"):
+            assert got[t][k] == ref[k], (t, k, got[t][k], ref[k])
+    # the small queries queued behind the large one ran first
+    later_small = set(tickets[5:])
+    assert any(finished.index(t) < finished.index(tickets[4]) for t in later_small)
+    srv.close()
+
+
 def _assert_results_match(res, refs, idx, keys=("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn")):
     for i, ref in zip(idx, refs):
         for k in keys:
