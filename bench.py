@@ -148,10 +148,10 @@ class ClockSampler:
 
 
 # DRAM traffic of k_propagate comes from an ncu capture of the current kernel
-# sources on a small case of this workload, summarised under profiles/ with
-# the hash of the sources it was taken on; a summary of other sources is
-# stale and gives no traffic figure (null).
-TRAFFIC_PROFILE = ROOT / "profiles" / "k_propagate_dram_batched_di64.md"
+# sources (three launches of this workload, one-pass metrics), summarised
+# under profiles/ with the hash of the sources it was taken on; a summary of
+# other sources is stale and gives no traffic figure (null).
+TRAFFIC_PROFILE = ROOT / "profiles" / "k_propagate_dram_batched_di256.md"
 KERNEL_SOURCES = ["kgmt_kernels.cu", "kgmt_iter.cuh", "kgmt_device.cuh", "kgmt_types.h"]
 
 
@@ -180,8 +180,8 @@ def propagate_traffic(samples_per_launch: float) -> dict:
         return {"traffic": None, "traffic_note": f"{TRAFFIC_PROFILE.name} was captured on other kernel sources"}
     b = float(per.group(1))
     return {"traffic": b * samples_per_launch, "traffic_bytes_per_sample": b,
-            "traffic_note": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per sample from {TRAFFIC_PROFILE.name} "
-                            f"(a small case of this workload, sources {sha.group(1)}), times this run's samples per launch"}
+            "traffic_note": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per sample on three main-phase launches of this "
+                            f"workload ({TRAFFIC_PROFILE.name}, sources {sha.group(1)}), times this run's samples per launch"}
 
 
 # algorithmic bytes of the double-integrator propagate: per sample the
