@@ -65,8 +65,10 @@ __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
     float r = fmaf(-n, 0x1.92p+0f, x);
     r = fmaf(-n, 0x1.fb4p-12f, r);
     r = fmaf(-n, 0x1.4442d2p-24f, r);
-    float qf = n - 4.0f * floorf(n * 0.25f);
-    int q = (qf >= 0.0f && qf <= 3.0f) ? (int)qf : 0;
+    // quadrant n mod 4 from the integer bits: the value n - 4 floor(n / 4)
+    // gives for every integer-valued |n| < 2^31, and 0 (as that form, clamped
+    // to [0, 3], gives) for larger |n|, NaN and infinity
+    const int q = fabsf(n) < 0x1p31f ? ((int)n & 3) : 0;
     float r2 = r * r;
     float ps = fmaf(r2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
     ps = fmaf(r2, ps, 0x1.111112p-7f);
@@ -79,8 +81,9 @@ __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
     float cp = fmaf(r2, pc, 1.0f);
     float ss = (q & 1) ? cp : sp;
     float cc = (q & 1) ? sp : cp;
-    s = (q == 2 || q == 3) ? -ss : ss;
-    c = (q == 1 || q == 2) ? -cc : cc;
+    // sine negative in quadrants 2 and 3, cosine in 1 and 2: sign-bit flips
+    s = __int_as_float(__float_as_int(ss) ^ ((q & 2) << 30));
+    c = __int_as_float(__float_as_int(cc) ^ (((q + 1) & 2) << 30));
 }
 
 // ---------------------------------------------------------------------------
