@@ -272,6 +272,41 @@ def test_batch_all_models_matches_oracle():
         assert np.array_equal(s[:n].view(np.uint32), alone[1].view(np.uint32))
 
 
+@pytest.mark.parametrize("kind", ["di2", "di3", "di4", "models4"])
+def test_tail_launch_matches_chain_and_oracle(kind, monkeypatch):
+    """Batches of 2-4 queries run whole iterations in the persistent tail
+    launch from the first iteration on (several running queries, then fewer
+    as they finish, then one: both ways of scoring regions); the plans equal
+    the oracle's, the trees equal those of the two-kernel chain alone
+    (KGMT_TAIL=0), and so do the step, box-test and sample counts."""
+    if kind == "models4":
+        qs = W.all_models_batch(4, seed=6, tree_capacity=20_000)
+        for q in qs:
+            q.config = q.config.replace(max_iterations=60)
+    else:
+        qs = W.double_integrator_batch(int(kind[2:]), n_obstacles=50, seed=11, tree_capacity=20_000)
+    b, res = _batch(qs)
+    st = b.stats()
+    assert st["iterations_tail"] > 0
+    monkeypatch.setenv("KGMT_TAIL", "0")
+    b0, res0 = _batch(qs)
+    st0 = b0.stats()
+    assert st0["iterations_tail"] == 0
+    refs = O.plan_batch(qs)
+    for i, (r, r0, ref) in enumerate(zip(res, res0, refs)):
+        for k in ("status", "iterations", "tree_size", "goal_index", "path_len", "samples_drawn"):
+            assert r[k] == ref[k] == r0[k], (kind, i, k, r[k], r0[k], ref[k])
+        s, p, c = b.copy_tree(i)
+        s0, p0, c0 = b0.copy_tree(i)
+        n = r["tree_size"]
+        assert np.array_equal(p[:n], p0[:n]) and np.array_equal(s[:n].view(np.uint32), s0[:n].view(np.uint32))
+        assert np.array_equal(c[:n].view(np.uint32), c0[:n].view(np.uint32))
+    for k in ("steps_executed", "obstacle_tests", "samples"):
+        assert st[k] == st0[k], (kind, k, st[k], st0[k])
+    b.close()
+    b0.close()
+
+
 def test_plan_edge_cases():
     # no obstacles
     q = W.double_integrator_query(seed=6)
