@@ -404,6 +404,7 @@ struct PropShared {
     uint32_t acc;                // accepted samples of the tile
     uint32_t steps;              // RK4 steps of the tile
     uint32_t tests;              // box tests of the tile
+    uint32_t next_run;           // runs of the sorted tile handed to warps so far
 };
 
 // sample rows of a model
@@ -584,13 +585,14 @@ __device__ __forceinline__ void finish_sample(const QueryParams& p, const GridVi
 // One propagate tile of `tile` samples of one query: tile <= NT (a power of
 // two) gives thread i < tile sample lt * tile + i; tile = kPropPer x NT gives
 // thread i samples (2 lt + h) * NT + i, h = 0, 1.  A counting sort of the tile
-// by step count (dead lanes last), then one pass per sample of a thread --
-// pass 0 gives thread i the i-th shortest sample, pass 1 the i-th longest, so
-// every thread gets about the same work and a warp's lanes loop about equally
-// long in each pass.  `wait` runs once, after pass 0 has gathered its parents
-// and draws (the boxes' bulk copy may be in flight until then).
-// Block-uniform call.  COHERENT: parent rows may have been appended by other
-// blocks earlier in the same launch (see load_row_ro).
+// by step count (dead lanes last), then the sorted tile in runs of 32
+// consecutive samples, one sample a lane: a warp takes the longest run left
+// whenever it is free (a shared counter), so the warps of a block finish the
+// tile together however early their samples end.  `wait` runs once per
+// thread, after its first run has gathered its parents and draws (the boxes'
+// bulk copy may be in flight until then).  Block-uniform call.  COHERENT:
+// parent rows may have been appended by other blocks earlier in the same
+// launch (see load_row_ro).
 template <int NT, int MODELS, bool COHERENT = false, typename Wait>
 __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const PropCtx& sc, uint32_t lt, uint32_t tile, uint32_t smem_boxes, PropShared* sh,
                                                uint32_t* s_hist, uint32_t* s_perm, uint4* s_key, const float4* s_obs, const uint16_t* s_gstart,
@@ -649,11 +651,21 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
         __syncthreads();
     }
     const float4* obs = sp.n_obstacles <= smem_boxes ? s_obs : sp.obstacles;
-    static_assert(kPropPer == 2, "the passes pair the i-th shortest with the i-th longest sample");
-    for(int pass = 0; pass < per; ++pass)
+    // live samples come first in the sorted order: the dead bin's start
+    const uint32_t n_live = s_hist[kSortBins - 1];
+    const uint32_t n_runs = (n_live + 31u) / 32u;
+    const unsigned full = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool waited = false;
+    for(;;)
         {
-            const uint32_t slot = pass == 0 ? threadIdx.x : (uint32_t)(2 * NT - 1) - threadIdx.x;
-            const uint32_t s = s_perm[slot];
+            uint32_t run = 0;
+            if(lane == 0) run = atomicAdd(&sh->next_run, 1u);
+            run = __shfl_sync(full, run, 0);
+            if(run >= n_runs) break;
+            // longest runs first
+            const uint32_t slot = (n_runs - 1u - run) * 32u + lane;
+            const uint32_t s = slot < n_live ? s_perm[slot] : 0xFFFFFFFFu;
             const bool live = s < sc.n_samples;
             float x0[KGMT_MAX_SAMPLE_DIM], u[8];
             uint32_t par = 0;
@@ -663,10 +675,16 @@ __device__ __forceinline__ void propagate_tile(const QueryParams& sp, const Prop
                     const U4 kb1{k4.x, k4.y, k4.z, k4.w};
                     with_model<MODELS>(model, [&](auto m) { par = prepare_sample<decltype(m)::value, COHERENT>(sp, sc, s, kb1, x0, u); });
                 }
-            if(pass == 0) wait();
+            if(!waited)
+                {
+                    wait();
+                    waited = true;
+                }
             const GridView grid{(sp.grid_meta != nullptr && s_gmeta[1] == 1u) ? s_gstart : nullptr, s_gitems, sp.grid_items};
             with_model<MODELS>(model, [&](auto m) { finish_sample<decltype(m)::value>(sp, grid, obs, sp.n_obstacles, s, live, par, x0, u, sh); });
         }
+    // a thread that got no run still follows the copy's phase
+    if(!waited) wait();
 }
 
 // Samples [s0, s0 + n) of one query, one per thread (n <= NT), in index

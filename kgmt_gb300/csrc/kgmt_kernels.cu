@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(NT, (MODELS == kBitDI ? 1024 : 512) / NT) k_pr
                 {
                     s_tile = (int)t;
                     s_q = t < total ? find_slot(bases.base, bases.n, t) : -1;
-                    s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0;
+                    s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0, s_sh.next_run = 0;
                     s_last = 0;
                     if(t < total) t_next = gridDim.x + atomicAdd(&sched->ticket_a, 1u);
                 }

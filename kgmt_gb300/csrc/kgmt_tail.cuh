@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_tail(const QueryParams* __r
                                 s_c.spe = tq[q].spe;
                                 s_c.n_react = tq[q].n_react;
                                 s_c.n_samples = ns;
-                                s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0;
+                                s_sh.acc = 0, s_sh.steps = 0, s_sh.tests = 0, s_sh.next_run = 0;
                             }
                         __syncthreads();
                         for(uint32_t r0 = lo; r0 < hi; r0 += NT)

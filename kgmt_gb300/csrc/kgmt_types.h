@@ -27,9 +27,10 @@ constexpr int kTileOldSmall = 1024;
 constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread, at most
 // samples per propagate thread and tile in iterations with enough samples to
 // fill the resident threads twice: a tile of kPropPer * NT samples is sorted
-// by step count and thread t runs the t-th shortest and the t-th longest, so
-// the threads of a block finish together.  Smaller iterations keep one sample
-// per thread (more tiles in parallel, a shorter chain per thread).
+// by step count and run 32 consecutive samples at a time, the longest first,
+// by whichever warp of the block is free, so the warps finish together.
+// Smaller iterations keep one sample per thread (more tiles in parallel, a
+// shorter chain per thread).
 constexpr int kPropPer = 2;
 constexpr int kRootRepeat = 5;          // KGMT.cu:67
 constexpr int kRepeatSparse = 15;       // KGMT.cu:336-337
