@@ -282,15 +282,17 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
             const int y0 = min(a.y, sc.y), y1 = max(a.y, sc.y);
             const int z0 = min(a.z, sc.z), z1 = max(a.z, sc.z);
             const int G = (int)P.grid_dim;
-            // cell coordinates are clamped to [0, G), so both loads stay in bounds
-            const int c0 = (x0 * G + y0) * G + z0;
-            uint32_t j = grid.start[c0];
-            const uint32_t e0 = grid.start[c0 + 1];
             const bool cells_ok = a.ok & sc.ok;
-            if(cells_ok & (x0 == x1) & (y0 == y1) & (z0 == z1))
+            // the common case, both end points in one cell, runs its own short
+            // loop only when it is every running lane's case: a warp whose
+            // lanes differ takes the cell-range loop below (the same boxes in
+            // the same order for a single cell) instead of running both
+            if(__all_sync(__activemask(), cells_ok & (x0 == x1) & (y0 == y1) & (z0 == z1)))
                 {
-                    // the common case: both end points in one cell
-                    for(; j < e0 && !hit; ++j)
+                    // cell coordinates are clamped to [0, G), so both loads stay in bounds
+                    const int c0 = (x0 * G + y0) * G + z0;
+                    const uint32_t e0 = grid.start[c0 + 1];
+                    for(uint32_t j = grid.start[c0]; j < e0 && !hit; ++j)
                         {
                             ++cnt.tests;
                             hit = PLANAR ? box_hit_xy(obs, grid_item(grid, j), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, j), lx, ly, lz, hx, hy, hz);
