@@ -302,19 +302,23 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
             const uint32_t n_cells = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1));
             if(cells_ok & (n_cells <= kGridMaxVisit))
                 {
-                    for(int cx = x0; cx <= x1 && !hit; ++cx)
-                        for(int cy = y0; cy <= y1 && !hit; ++cy)
-                            for(int cz = z0; cz <= z1 && !hit; ++cz)
+                    // the cells in x, y, z order (z fastest) as one loop: lanes
+                    // with different cell ranges part at one loop, not three
+                    int cx = x0, cy = y0, cz = z0;
+                    for(uint32_t ci = 0; ci < n_cells && !hit; ++ci)
+                        {
+                            const int c = (cx * G + cy) * G + cz;
+                            const uint32_t e = grid.start[c + 1];
+                            for(uint32_t k = grid.start[c]; k < e && !hit; ++k)
                                 {
-                                    const int c = (cx * G + cy) * G + cz;
-                                    const uint32_t e = grid.start[c + 1];
-                                    for(uint32_t k = grid.start[c]; k < e && !hit; ++k)
-                                        {
-                                            ++cnt.tests;
-                                            hit = PLANAR ? box_hit_xy(obs, grid_item(grid, k), lx, ly, hx, hy)
-                                                         : box_hit(obs, grid_item(grid, k), lx, ly, lz, hx, hy, hz);
-                                        }
+                                    ++cnt.tests;
+                                    hit = PLANAR ? box_hit_xy(obs, grid_item(grid, k), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, k), lx, ly, lz, hx, hy, hz);
                                 }
+                            const bool wz = cz < z1, wy = cy < y1;
+                            cz = wz ? cz + 1 : z0;
+                            cy = wz ? cy : (wy ? cy + 1 : y0);
+                            cx = (wz | wy) ? cx : cx + 1;
+                        }
                     return !hit;
                 }
         }
