@@ -60,15 +60,19 @@ __device__ __forceinline__ float u01(uint32_t x) { return (float)((x >> 8) + 1u)
 __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
 {
     // explicit fused multiply-adds (one rounding each), placed exactly as in
-    // the CPU restatement; nothing else is contracted (-fmad=false)
-    float n = rintf(x * 0x1.45f306p-1f);
+    // the CPU restatement; nothing else is contracted (-fmad=false).
+    // The nearest multiple n of pi/2 by adding 1.5 * 2^23: while
+    // |x * 2/pi| < 2^22 the sum rounds to an integer exactly as rintf does
+    // (to nearest, ties to even), subtracting the constant again gives n
+    // exactly, and the sum's two lowest bits are n mod 4, the quadrant.
+    // Beyond that range (where the reduction means nothing) both sides still
+    // compute the same values.
+    const float t = x * 0x1.45f306p-1f + 0x1.8p23f;
+    const float n = t - 0x1.8p23f;
+    const int q = __float_as_int(t) & 3;
     float r = fmaf(-n, 0x1.92p+0f, x);
     r = fmaf(-n, 0x1.fb4p-12f, r);
     r = fmaf(-n, 0x1.4442d2p-24f, r);
-    // quadrant n mod 4 from the integer bits: the value n - 4 floor(n / 4)
-    // gives for every integer-valued |n| < 2^31, and 0 (as that form, clamped
-    // to [0, 3], gives) for larger |n|, NaN and infinity
-    const int q = fabsf(n) < 0x1p31f ? ((int)n & 3) : 0;
     float r2 = r * r;
     float ps = fmaf(r2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
     ps = fmaf(r2, ps, 0x1.111112p-7f);

@@ -120,12 +120,18 @@ void ko_sincosf(float x, float* s_out, float* c_out)
 {
     /* fused multiply-adds (fmaf, one rounding each) in the same places as the
      * CUDA kernels */
-    float n = rintf(x * KO_TWO_OVER_PI);
+    /* n = nearest integer to x * 2/pi by adding 1.5 * 2^23 (the sum rounds to
+     * an integer as rintf does while |x * 2/pi| < 2^22; beyond, the same
+     * value as the kernels); the sum's two lowest bits are n mod 4 */
+    float t = x * KO_TWO_OVER_PI;
+    t = t + 0x1.8p23f;
+    float n = t - 0x1.8p23f;
+    uint32_t tb;
+    memcpy(&tb, &t, sizeof tb);
+    int q = (int)(tb & 3u);
     float r = fmaf(-n, KO_PIO2_1, x);
     r = fmaf(-n, KO_PIO2_2, r);
     r = fmaf(-n, KO_PIO2_3, r);
-    float qf = n - 4.0f * floorf(n * 0.25f);
-    int q = (qf >= 0.0f && qf <= 3.0f) ? (int)qf : 0;
     float r2 = r * r;
     float ps = fmaf(r2, KO_S4, KO_S3);
     ps = fmaf(r2, ps, KO_S2);

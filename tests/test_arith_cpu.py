@@ -30,29 +30,25 @@ def test_portable_sincos_accuracy():
     assert err_s < 2.4e-7 and err_c < 2.4e-7
 
 
-def test_sincos_quadrant_from_integer_bits():
-    """The kernels take the sine/cosine quadrant as (int)n & 3 (0 when
-    |n| >= 2^31, NaN or infinite); the oracle as n - 4 floor(n / 4) clamped
-    to [0, 3].  The two agree for every n = rint(x * 2/pi) (checked here over
-    random reductions, every integer near the float-spacing changes, and the
-    special values), so both sides pick the same polynomial and signs."""
+def test_sincos_rounding_by_magic_addition():
+    """Both sides take n = rint(x * 2/pi) as (x * 2/pi + 1.5 * 2^23) - 1.5 * 2^23
+    and the quadrant as the sum's two lowest bits.  While |x * 2/pi| < 2^22
+    (every angle the planners meet) that is rintf's round-to-nearest-even and
+    n mod 4 exactly: checked over random and hand-picked reductions, the ties
+    and the ends of the range."""
     rng = np.random.default_rng(7)
-    x = np.concatenate([rng.uniform(-1e4, 1e4, 200_000), rng.uniform(-3e9, 3e9, 50_000),
-                        rng.standard_normal(50_000) * 1e12]).astype(np.float32)
-    n = np.rint(x * np.float32(float.fromhex('0x1.45f306p-1'))).astype(np.float32)
-    edges = []
-    for e in (24, 25, 30, 31, 32):
-        for sgn in (1.0, -1.0):
-            for direction in (np.inf, -np.inf):
-                v = np.float32(sgn * 2.0 ** e)
-                for _ in range(9):
-                    edges.append(v)
-                    v = np.nextafter(v, np.float32(direction))
-    n = np.concatenate([n, np.float32(edges), np.arange(-100, 101, dtype=np.float32),
-                        np.float32([np.nan, np.inf, -np.inf, 0.0, -0.0])])
-    with np.errstate(invalid="ignore"):
-        qf = (n - np.float32(4.0) * np.floor(n * np.float32(0.25))).astype(np.float32)
-        q_float = np.where((qf >= 0) & (qf <= 3), np.nan_to_num(qf).astype(np.int64), 0)
-        small = np.abs(n) < np.float32(2.0 ** 31)
-        q_int = np.where(small, np.where(small, n, 0).astype(np.int64) & 3, 0)
-    assert np.array_equal(q_float, q_int)
+    f32 = np.float32
+    two_over_pi = f32(float.fromhex('0x1.45f306p-1'))
+    magic = f32(1.5 * 2.0 ** 23)
+    x = np.concatenate([rng.uniform(-1e4, 1e4, 200_000), rng.uniform(-6.5e6, 6.5e6, 100_000),
+                        np.arange(-200, 201) * (np.pi / 4)]).astype(f32)
+    y = (x * two_over_pi).astype(f32)
+    # ties and the range ends, as products
+    ties = np.concatenate([np.arange(-64, 64) + f32(0.5), np.float32([2.0 ** 22 - 1, -(2.0 ** 22 - 1), 2.0 ** 22 - 0.5, -(2.0 ** 22 - 0.5)])])
+    y = np.concatenate([y, ties.astype(f32)])
+    y = y[np.abs(y) < f32(2.0 ** 22)]
+    t = (y + magic).astype(f32)
+    n = (t - magic).astype(f32)
+    assert np.array_equal(n, np.rint(y).astype(f32))
+    q = t.view(np.uint32) & 3
+    assert np.array_equal(q.astype(np.int64), np.rint(y).astype(np.int64) & 3)
