@@ -306,22 +306,24 @@ __device__ __forceinline__ bool step_free(const QueryParams& P, const GridView& 
             const uint32_t n_cells = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1));
             if(cells_ok & (n_cells <= kGridMaxVisit))
                 {
-                    // the cells in x, y, z order (z fastest) as one loop: lanes
-                    // with different cell ranges part at one loop, not three
-                    int cx = x0, cy = y0, cz = z0;
-                    for(uint32_t ci = 0; ci < n_cells && !hit; ++ci)
+                    // the cells in x, y, z order (z fastest) as one loop over
+                    // the (x, y) columns: the item lists of a column's cells
+                    // z0..z1 lie back to back, so each column is one range
+                    // (lanes with different cell ranges part at one loop, not three)
+                    const uint32_t n_cols = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+                    int cx = x0, cy = y0;
+                    for(uint32_t ci = 0; ci < n_cols && !hit; ++ci)
                         {
-                            const int c = (cx * G + cy) * G + cz;
-                            const uint32_t e = grid.start[c + 1];
+                            const int c = (cx * G + cy) * G + z0;
+                            const uint32_t e = grid.start[c + (z1 - z0) + 1];
                             for(uint32_t k = grid.start[c]; k < e && !hit; ++k)
                                 {
                                     ++cnt.tests;
                                     hit = PLANAR ? box_hit_xy(obs, grid_item(grid, k), lx, ly, hx, hy) : box_hit(obs, grid_item(grid, k), lx, ly, lz, hx, hy, hz);
                                 }
-                            const bool wz = cz < z1, wy = cy < y1;
-                            cz = wz ? cz + 1 : z0;
-                            cy = wz ? cy : (wy ? cy + 1 : y0);
-                            cx = (wz | wy) ? cx : cx + 1;
+                            const bool wy = cy < y1;
+                            cy = wy ? cy + 1 : y0;
+                            cx = wy ? cx : cx + 1;
                         }
                     return !hit;
                 }
