@@ -52,10 +52,12 @@ __device__ __forceinline__ float u01(uint32_t x) { return (float)((x >> 8) + 1u)
 
 // ---------------------------------------------------------------------------
 // Portable sine/cosine: Cody & Waite reduction by pi/2 (three-part split,
-// n*P1 and n*P2 exact for |n| < 2^13) and Taylor polynomials (degree 9 / 10)
-// on |r| <= pi/4, Horner form, coefficients 1/n! rounded to float.  Written
-// from the series so the CPU restatement rounds identically; accuracy about
-// one ulp for |x| < 1e4.
+// n*P1 and n*P2 exact for |n| < 2^13) and minimax polynomials on |r| <= pi/4
+// in Horner form: sin r = r + r^3 (s1 + s2 r^2 + s3 r^4), cos r = 1 - r^2/2
+// + r^4 (c2 + c3 r^2 + c4 r^4), fitted by Lawson's iteratively reweighted
+// least squares to relative errors 3.8e-9 and 1.2e-10 and rounded to float
+// (oracle/fit_sincos.py).  Same operations as the CPU restatement, so both
+// round identically; accuracy about one ulp for |x| < 1e4.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
 {
@@ -74,13 +76,11 @@ __device__ __forceinline__ void sincos_portable(float x, float& s, float& c)
     r = fmaf(-n, 0x1.fb4p-12f, r);
     r = fmaf(-n, 0x1.4442d2p-24f, r);
     float r2 = r * r;
-    float ps = fmaf(r2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
-    ps = fmaf(r2, ps, 0x1.111112p-7f);
-    ps = fmaf(r2, ps, -0x1.555556p-3f);
+    float ps = fmaf(r2, -0x1.9943ep-13f, 0x1.11073ap-7f);
+    ps = fmaf(r2, ps, -0x1.555546p-3f);
     float sp = fmaf(r * r2, ps, r);
-    float pc = fmaf(r2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
-    pc = fmaf(r2, pc, -0x1.6c16c2p-10f);
-    pc = fmaf(r2, pc, 0x1.555556p-5f);
+    float pc = fmaf(r2, 0x1.99eba6p-16f, -0x1.6c0c34p-10f);
+    pc = fmaf(r2, pc, 0x1.55554ap-5f);
     pc = fmaf(r2, pc, -0x1.0p-1f);
     float cp = fmaf(r2, pc, 1.0f);
     float ss = (q & 1) ? cp : sp;

@@ -97,24 +97,24 @@ float ko_react_uniform(uint64_t seed, uint32_t node, uint32_t itr)
 /* ------------------------------------------------------------------------ */
 /* Portable single-precision sine/cosine.  Cody & Waite argument reduction   */
 /* by pi/2 split in three parts (first two short enough that n*P1 and n*P2   */
-/* are exact for |n| < 2^13), then Taylor polynomials of degree 9 (sin) and  */
-/* 10 (cos) on |r| <= pi/4 evaluated in Horner form.  Coefficients are 1/n!  */
-/* rounded to float.  Same operations, same order on CPU and GPU, so both    */
-/* round identically.                                                        */
+/* are exact for |n| < 2^13), then minimax polynomials on |r| <= pi/4 in     */
+/* Horner form: sin r = r + r^3 (S1 + S2 r^2 + S3 r^4) and                   */
+/* cos r = 1 - r^2/2 + r^4 (C2 + C3 r^2 + C4 r^4), fitted by Lawson's        */
+/* iteratively reweighted least squares (fit_sincos.py) and rounded to      */
+/* float.  Same operations, same order on CPU and GPU, so both round        */
+/* identically.                                                              */
 /* ------------------------------------------------------------------------ */
 #define KO_TWO_OVER_PI 0x1.45f306p-1f
 #define KO_PIO2_1 0x1.92p+0f
 #define KO_PIO2_2 0x1.fb4p-12f
 #define KO_PIO2_3 0x1.4442d2p-24f
-#define KO_S1 (-0x1.555556p-3f) /* -1/3!  */
-#define KO_S2 0x1.111112p-7f    /*  1/5!  */
-#define KO_S3 (-0x1.a01a02p-13f)/* -1/7!  */
-#define KO_S4 0x1.71de3ap-19f   /*  1/9!  */
-#define KO_C1 (-0x1.0p-1f)      /* -1/2!  */
-#define KO_C2 0x1.555556p-5f    /*  1/4!  */
-#define KO_C3 (-0x1.6c16c2p-10f)/* -1/6!  */
-#define KO_C4 0x1.a01a02p-16f   /*  1/8!  */
-#define KO_C5 (-0x1.27e4fcp-22f)/* -1/10! */
+#define KO_S1 (-0x1.555546p-3f)
+#define KO_S2 0x1.11073ap-7f
+#define KO_S3 (-0x1.9943ep-13f)
+#define KO_C1 (-0x1.0p-1f)
+#define KO_C2 0x1.55554ap-5f
+#define KO_C3 (-0x1.6c0c34p-10f)
+#define KO_C4 0x1.99eba6p-16f
 
 void ko_sincosf(float x, float* s_out, float* c_out)
 {
@@ -133,12 +133,10 @@ void ko_sincosf(float x, float* s_out, float* c_out)
     r = fmaf(-n, KO_PIO2_2, r);
     r = fmaf(-n, KO_PIO2_3, r);
     float r2 = r * r;
-    float ps = fmaf(r2, KO_S4, KO_S3);
-    ps = fmaf(r2, ps, KO_S2);
+    float ps = fmaf(r2, KO_S3, KO_S2);
     ps = fmaf(r2, ps, KO_S1);
     float sp = fmaf(r * r2, ps, r);
-    float pc = fmaf(r2, KO_C5, KO_C4);
-    pc = fmaf(r2, pc, KO_C3);
+    float pc = fmaf(r2, KO_C4, KO_C3);
     pc = fmaf(r2, pc, KO_C2);
     pc = fmaf(r2, pc, KO_C1);
     float cp = fmaf(r2, pc, 1.0f);
