@@ -150,9 +150,6 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_tail(const QueryParams* __r
     __shared__ PropCtx s_c;
     __shared__ PropShared s_sh;
     __shared__ float s_lanes[kScoreLanes];
-    __shared__ uint32_t s_hist[kSortBins];
-    __shared__ uint32_t s_perm[kPropPer * NT];
-    __shared__ uint4 s_key[kPropPer * NT];
     __shared__ uint32_t s_scan[34];
     __shared__ uint32_t s_sum[NT / 32][6];
     __shared__ TailQuery tq[kTailQueries];
