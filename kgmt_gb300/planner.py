@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import KgmtBatchOptions, KgmtResult, KgmtServerOptions, check, load, ptr, to_c
-from .config import MAX_SAMPLE_DIM, PlannerConfig, sample_dim
+from .config import PlannerConfig
 
 
 def _f32(a) -> np.ndarray:
