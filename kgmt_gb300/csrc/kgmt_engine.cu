@@ -203,7 +203,11 @@ QueryLayout layout_of(const kgmt_config& c, uint32_t n_obstacles, bool inline_ob
     L.grid_budget = n_obstacles ? std::min<uint32_t>(kMaxGridItems, std::max<uint32_t>(8192u, 32u * std::min(n_obstacles, 4096u))) : 0u;
     const size_t T = c.tree_capacity, D = sample_dim_of(c.model);
     const size_t R1 = regions_of(c);
-    L.tiles_per_chain = (uint32_t)((T + kTileC - 1) / kTileC + 1);
+    // look-back words of the two chains, one per tile of the smallest size
+    // either uses (re-activation tiles of kTileOldSmall old nodes, append
+    // tiles of kTileC samples)
+    constexpr uint64_t kMinTile = (uint64_t)(kTileC < kTileOldSmall ? kTileC : kTileOldSmall);
+    L.tiles_per_chain = (uint32_t)((T + kMinTile - 1) / kMinTile + 1);
     size_t cur = 0;
     L.tree = aligned(cur, T * D * 4);
     L.parent = aligned(cur, T * 4);

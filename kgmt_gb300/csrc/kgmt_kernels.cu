@@ -537,46 +537,43 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
             else
                 {
                     // ---- ordered append of accepted samples (KGMT.cu:317-362) ----
+                    // kAppendPer consecutive samples a thread: their
+                    // region-and-flag words four at a time (s0 is a multiple
+                    // of 4: 16-byte loads), then the accepted samples' valid
+                    // counts -- two round trips; only the flag bits are kept
+                    // past the scan (the scatter reads the word again)
                     const uint32_t lts = lt - n_old;
                     const uint32_t s0 = lts * kTileC + threadIdx.x * kAppendPer;
                     const uint32_t ns = st.n_samples;
-                    uint32_t acc_bits = 0, ca = 0, cw = 0;
-                    // region-and-flag words of the thread's samples (s0 is a
-                    // multiple of 4: one 16-byte load), then the accepted
-                    // samples' valid counts: two round trips
-                    static_assert(kAppendPer == 4, "one 16-byte load of four region-and-flag words");
-                    uint32_t fl[kAppendPer];
-                    int32_t rg[kAppendPer];
+                    static_assert(kAppendPer % 4 == 0 && kAppendPer <= 32, "16-byte loads of four words, one flag bit per sample");
+                    static_assert(kTileC * kRepeatSparse < 65536, "a tile's repeat count fits the scan's low 16 bits");
                     uint32_t rf[kAppendPer];
-                    if(s0 + 3 < ns)
-                        {
-                            const uint4 v = *(const uint4*)(p.ur1f + s0);
-                            rf[0] = v.x, rf[1] = v.y, rf[2] = v.z, rf[3] = v.w;
-                        }
-                    else
-                        {
 #pragma unroll
-                            for(int j = 0; j < kAppendPer; ++j) rf[j] = s0 + j < ns ? p.ur1f[s0 + j] : 0u;
-                        }
-#pragma unroll
-                    for(int j = 0; j < kAppendPer; ++j)
+                    for(int g = 0; g < kAppendPer; g += 4)
                         {
-                            fl[j] = rf[j] >> 31;
-                            rg[j] = (int32_t)(rf[j] & 0x7FFFFFFFu);
-                        }
-                    uint32_t w[kAppendPer];
-#pragma unroll
-                    for(int j = 0; j < kAppendPer; ++j)
-                        {
-                            w[j] = 0;
-                            if(fl[j])
+                            const uint32_t sb = s0 + g;
+                            if(sb + 3 < ns)
                                 {
-                                    acc_bits |= 1u << j;
-                                    ++ca;
-                                    w[j] = p.valid[rg[j]] < kSparseValidLimit ? kRepeatSparse : kRepeatDense;
-                                    cw += w[j];
+                                    const uint4 v = *(const uint4*)(p.ur1f + sb);
+                                    rf[g] = v.x, rf[g + 1] = v.y, rf[g + 2] = v.z, rf[g + 3] = v.w;
+                                }
+                            else
+                                {
+#pragma unroll
+                                    for(int j = 0; j < 4; ++j) rf[g + j] = sb + j < ns ? p.ur1f[sb + j] : 0u;
                                 }
                         }
+                    uint32_t acc_bits = 0, sparse_bits = 0, ca = 0, cw = 0;
+#pragma unroll
+                    for(int j = 0; j < kAppendPer; ++j)
+                        if(rf[j] >> 31)
+                            {
+                                const bool sparse = p.valid[rf[j] & 0x7FFFFFFFu] < kSparseValidLimit;
+                                acc_bits |= 1u << j;
+                                sparse_bits |= sparse ? 1u << j : 0u;
+                                ++ca;
+                                cw += sparse ? kRepeatSparse : kRepeatDense;
+                            }
                     uint32_t agg;
                     const uint32_t excl = block_exclusive_scan<kAppendThreads>((ca << 16) | cw, scratch, &agg);
                     const uint32_t agg_a = agg >> 16, agg_w = agg & 0xffffu;
@@ -592,21 +589,25 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
                     uint32_t ia = tree_size + (uint32_t)(pre >> 32) + (excl >> 16);
                     uint32_t iw = (uint32_t)(pre & 0xffffffffull) + (excl & 0xffffu);
                     const int D = (int)p.sample_dim;
-#pragma unroll
-                    for(int j = 0; j < kAppendPer; ++j)
+                    for(uint32_t m = acc_bits; m; m &= m - 1u)
                         {
-                            if(!(acc_bits & (1u << j))) continue;
-                            const uint32_t s = s0 + j;
+                            const int j = __ffs((int)m) - 1;
+                            const uint32_t s = s0 + (uint32_t)j;
                             const uint32_t idx = ia++;
-                            if(!KGMT_BOUND(idx < p.capacity && s < p.capacity)) continue;
+                            const uint32_t w = ((sparse_bits >> j) & 1u) ? kRepeatSparse : kRepeatDense;
+                            if(!KGMT_BOUND(idx < p.capacity && s < p.capacity))
+                                {
+                                    iw += w;
+                                    continue;
+                                }
                             // everything the sample needs is loaded before its
                             // first store (one round trip, not one per field)
-                            const int32_t par = __ldg(p.up + s), r1 = rg[j];
+                            const int32_t par = __ldg(p.up + s), r1 = (int32_t)(__ldg(p.ur1f + s) & 0x7FFFFFFFu);
                             const float dist = append_row(p, p.us + (size_t)s * D, p.tree + (size_t)idx * D, D);
                             p.parent[idx] = par;
                             p.cost[idx] = dist;
                             p.node_r1[idx] = r1;
-                            for(uint32_t r = 0; r < w[j]; ++r, ++iw)
+                            for(uint32_t r = 0; r < w; ++r, ++iw)
                                 if(iw < p.capacity) p.rep_new[iw] = idx;
                             if(dist < p.goal_radius) atomicMin(&st.goal_cand, (int)idx);
                         }
