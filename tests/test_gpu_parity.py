@@ -133,6 +133,40 @@ def test_propagate_quad_bit_exact_vs_oracle():
     assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
 
 
+def _same_bits_or_both_nan(a, b):
+    # a NaN's payload is the platform's (the GPU's canonical NaN is not the
+    # CPU's); every other value must match bit for bit
+    nan = np.isnan(a) | np.isnan(b)
+    return np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~nan].view(np.uint32), b[~nan].view(np.uint32))
+
+
+@pytest.mark.parametrize("model", ["quad", "dubins"])
+def test_propagate_large_angles_bit_exact_vs_oracle(model):
+    """Angles far outside one turn (|x| up to 1e4 rad): the portable
+    sine/cosine takes the nearest multiple of pi/2 and its quadrant from one
+    1.5 * 2^23 addition on both sides, so every quadrant and sign comes out
+    the same on the GPU and in the oracle."""
+    if model == "quad":
+        q = W.quadrotor_query(seed=3)
+        cfg = q.config
+        x0, u = random_inputs(cfg, 4096, 21)
+        rng = np.random.default_rng(5)
+        x0[:, 3:6] = rng.uniform(-100.0, 100.0, (4096, 3))
+        x0[:256, 3:6] = rng.uniform(-1e4, 1e4, (256, 3))
+    else:
+        q = W.dubins_query(seed=3)
+        cfg = q.config
+        x0, u = random_inputs(cfg, 4096, 22)
+        rng = np.random.default_rng(6)
+        x0[:, 3] = rng.uniform(-1e3, 1e3, 4096)
+        x0[:256, 3] = rng.uniform(-1e4, 1e4, 256)
+    gx, gv, g1, g2 = gpu_propagate(cfg, x0, u, q.obstacles)
+    ox, ov, o1, o2 = O.propagate_f32(cfg, x0, u, q.obstacles)
+    assert np.array_equal(gv, ov)
+    assert _same_bits_or_both_nan(gx, ox)
+    assert np.array_equal(g1, o1) and np.array_equal(g2, o2)
+
+
 @pytest.mark.parametrize("make", [W.dubins_query, W.unicycle_query], ids=["dubins", "unicycle"])
 def test_propagate_new_models_bit_exact_vs_oracle(make):
     q = make(seed=2, n_obstacles=40)
