@@ -238,9 +238,14 @@ __device__ void compute_schedule(const QueryParams* __restrict__ P, const QueryS
         return t;
     };
     // old nodes per re-activation tile: small tiles while the old nodes of
-    // all running queries fill fewer large tiles than there are SMs
+    // all running queries fill fewer tiles than there are SMs, large ones
+    // while they fill many waves of large tiles (each tile's fixed latency --
+    // loads, scan, look-back -- spread over more nodes)
     auto old_tile_for = [&](uint32_t tree_total) -> uint32_t {
-        return (sms != 0 && tree_total <= sms * (uint32_t)kTileOld) ? (uint32_t)kTileOldSmall : (uint32_t)kTileOld;
+        if(sms != 0 && tree_total <= sms * (uint32_t)kTileOld) return (uint32_t)kTileOldSmall;
+        if(sms != 0 && (unsigned long long)tree_total >= (unsigned long long)kOldLargeWaves * sms * (uint32_t)kTileOldLarge)
+            return (uint32_t)kTileOldLarge;
+        return (uint32_t)kTileOld;
     };
     // a slot's samples and tree size if it runs (three independent loads:
     // other blocks finalised these states in this kernel, so past L1)

@@ -479,60 +479,64 @@ __global__ void __launch_bounds__(kAppendThreads, 8) k_append(const QueryParams*
             if(lt < n_old)
                 {
                     // ---- re-activation of old nodes (KGMT.cu:364-377) ----
-                    // old_tile / kAppendThreads consecutive nodes a thread (4 or 16)
+                    // old_tile / kAppendThreads consecutive nodes a thread (4,
+                    // 16 or 32), in rounds of at most kOldPer
                     const uint32_t per_t = old_tile / kAppendThreads;
                     const uint32_t i0 = lt * old_tile + threadIdx.x * per_t;
                     const float fa = s_fa;
                     const uint32_t k0 = (uint32_t)p.seed, k1 = (uint32_t)(p.seed >> 32);
                     uint32_t flags = 0, cnt = 0;
-                    // node regions four at a time (i0 is a multiple of 4: the
-                    // 16-byte loads are aligned), then the region scores
-                    static_assert(kOldPer % 4 == 0 && kOldPer <= 32, "re-activation: 4-node loads, one flag bit per node");
-                    int32_t reg[kOldPer];
+                    static_assert(kOldPer % 4 == 0 && kTileOldLarge / kAppendThreads <= 32, "re-activation: 4-node loads, one flag bit per node");
+                    // one round: kOldPer nodes from i0 + r0 -- their regions
+                    // four at a time (i0 + r0 is a multiple of 4: the 16-byte
+                    // loads are aligned), then the region scores
+                    auto round = [&](uint32_t r0) {
+                        int32_t reg[kOldPer];
 #pragma unroll
-                    for(int g = 0; g < kOldPer; g += 4)
-                        {
-                            const uint32_t ib = i0 + g;
-                            if((uint32_t)g >= per_t) reg[g] = reg[g + 1] = reg[g + 2] = reg[g + 3] = 0;
-                            else if(ib + 3 < tree_size)
-                                {
-                                    const int4 v = *(const int4*)(p.node_r1 + ib);
-                                    reg[g] = v.x, reg[g + 1] = v.y, reg[g + 2] = v.z, reg[g + 3] = v.w;
-                                }
-                            else
-                                {
+                        for(int g = 0; g < kOldPer; g += 4)
+                            {
+                                const uint32_t ib = i0 + r0 + g;
+                                if(r0 + g >= per_t) reg[g] = reg[g + 1] = reg[g + 2] = reg[g + 3] = 0;
+                                else if(ib + 3 < tree_size)
+                                    {
+                                        const int4 v = *(const int4*)(p.node_r1 + ib);
+                                        reg[g] = v.x, reg[g + 1] = v.y, reg[g + 2] = v.z, reg[g + 3] = v.w;
+                                    }
+                                else
+                                    {
 #pragma unroll
-                                    for(int j = 0; j < 4; ++j) reg[g + j] = ib + j < tree_size ? p.node_r1[ib + j] : 0;
-                                }
-                        }
+                                        for(int j = 0; j < 4; ++j) reg[g + j] = ib + j < tree_size ? p.node_r1[ib + j] : 0;
+                                    }
+                            }
 #pragma unroll
-                    for(int j = 0; j < kOldPer; ++j)
-                        {
-                            const uint32_t i = i0 + j;
-                            if((uint32_t)j < per_t && i < tree_size)
-                                {
-                                    const U4 r = philox4x32_10(i, itr, 1u, 0u, k0, k1);
-                                    const float ur = u01(r.x);
-                                    if(ur <= p.score[reg[j]] + fa)
-                                        {
-                                            flags |= 1u << j;
-                                            ++cnt;
-                                        }
-                                }
-                        }
+                        for(int j = 0; j < kOldPer; ++j)
+                            {
+                                const uint32_t i = i0 + r0 + j;
+                                if(r0 + j < per_t && i < tree_size)
+                                    {
+                                        const U4 r = philox4x32_10(i, itr, 1u, 0u, k0, k1);
+                                        const float ur = u01(r.x);
+                                        if(ur <= p.score[reg[j]] + fa)
+                                            {
+                                                flags |= 1u << (r0 + j);
+                                                ++cnt;
+                                            }
+                                    }
+                            }
+                    };
+                    round(0u);
+                    if(per_t > (uint32_t)kOldPer) round((uint32_t)kOldPer);
                     uint32_t agg;
                     const uint32_t excl = block_exclusive_scan<kAppendThreads>(cnt, scratch, &agg);
                     publish_and_lookback(p.tiles_old, lt, agg, &s_prefix, &sched->error);
                     if(threadIdx.x == 0) atomicAdd(&st.react_total, agg);
                     __syncthreads();
                     uint32_t pos = (uint32_t)s_prefix + excl;
-#pragma unroll
-                    for(int j = 0; j < kOldPer; ++j)
-                        if(flags & (1u << j))
-                            {
-                                if(KGMT_BOUND(pos < p.capacity)) p.rep_old[pos] = i0 + j;
-                                ++pos;
-                            }
+                    for(uint32_t m = flags; m; m &= m - 1u)
+                        {
+                            if(KGMT_BOUND(pos < p.capacity)) p.rep_old[pos] = i0 + (uint32_t)(__ffs((int)m) - 1);
+                            ++pos;
+                        }
                 }
             else
                 {

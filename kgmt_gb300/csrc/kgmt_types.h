@@ -24,7 +24,11 @@ constexpr int kAppendPer = kTileC / kAppendThreads;  // samples per append threa
 // fewer large tiles than there are SMs, so few trees still spread out
 constexpr int kTileOld = 4096;
 constexpr int kTileOldSmall = 1024;
-constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread, at most
+constexpr int kTileOldLarge = 8192;
+constexpr int kOldPer = kTileOld / kAppendThreads;  // old nodes per thread and round, at most
+// iterations whose running trees hold at least this many large tiles per SM
+// use large re-activation tiles (two rounds of kOldPer nodes a thread)
+constexpr uint32_t kOldLargeWaves = 8;
 // samples per propagate thread and tile in iterations with enough samples to
 // fill the resident threads twice: a tile of kPropPer * NT samples is sorted
 // by step count and run 32 consecutive samples at a time, the longest first,
