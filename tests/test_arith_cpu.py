@@ -52,3 +52,38 @@ def test_sincos_rounding_by_magic_addition():
     assert np.array_equal(n, np.rint(y).astype(f32))
     q = t.view(np.uint32) & 3
     assert np.array_equal(q.astype(np.int64), np.rint(y).astype(np.int64) & 3)
+
+
+def test_sincos_coefficients_come_from_the_fit():
+    """The minimax coefficients in the oracle (and, operation for operation,
+    in the kernels) are the float roundings of the Lawson fit in
+    oracle/fit_sincos.py, and that fit stays under 4e-9 / 2e-10 relative
+    error before rounding."""
+    import re
+    from pathlib import Path
+    import importlib.util
+    root = Path(__file__).resolve().parents[1]
+    spec = importlib.util.spec_from_file_location("fit_sincos", root / "oracle" / "fit_sincos.py")
+    fit = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fit)
+    half = np.pi / 8
+    x = np.cos(np.linspace(0.0, np.pi, 20001)) * half + half
+    x = x[x > 1e-6]
+    basis = np.stack([np.ones_like(x), x ** 2, x ** 4], 1)
+    cs, es = fit.lawson(basis, (np.sin(x) - x) / x ** 3, x ** 3 / np.sin(x))
+    cc, ec = fit.lawson(basis, (np.cos(x) - 1.0 + x ** 2 / 2.0) / x ** 4, x ** 4 / np.cos(x))
+    assert es < 4e-9 and ec < 2e-10
+    src = (root / "oracle" / "kgmt_oracle.c").read_text()
+    def const(name):
+        m = re.search(r"#define %s \(?(-?0x[0-9a-fp.+-]+)f\)?" % name, src)
+        return np.float32(float.fromhex(m.group(1)))
+    assert [const(n) for n in ("KO_S1", "KO_S2", "KO_S3")] == [np.float32(v) for v in cs]
+    assert [const(n) for n in ("KO_C2", "KO_C3", "KO_C4")] == [np.float32(v) for v in cc]
+    assert const("KO_C1") == np.float32(-0.5)
+    # the kernels' portable sine/cosine uses the same literals
+    dev = (root / "kgmt_gb300" / "csrc" / "kgmt_device.cuh").read_text()
+    body = dev[dev.index("void sincos_portable("):]
+    body = body[:body.index("\n}\n")]
+    lits = {np.float32(float.fromhex(m)) for m in re.findall(r"(-?0x[0-9a-f]\.[0-9a-f]+p[+-]?[0-9]+)f", body)}
+    for name in ("KO_S1", "KO_S2", "KO_S3", "KO_C1", "KO_C2", "KO_C3", "KO_C4"):
+        assert const(name) in lits, name
